@@ -92,6 +92,8 @@ def lib():
         L.orc_step.argtypes = [C.POINTER(Integrator), C.POINTER(C.c_double), u32p, P, P, P, P, P]
         L.orc_check_collision.argtypes = [C.c_int, C.c_double, C.c_double, C.c_uint32, P, P, P, P,
                                           P, C.c_uint32, u32p]
+        L.orc_check_collision_mt.argtypes = [C.c_int, C.c_double, C.c_double, C.c_uint32, P, P, P, P,
+                                             P, C.c_uint32, u32p, C.c_int]
         L.orc_check_ejection_hit_centrum.argtypes = [C.c_double, C.c_double, C.c_double, C.c_uint32,
                                                      P, P, P, P, P, C.c_uint32, u32p]
         L.orc_populate_sp_events.argtypes = [P, C.c_uint32]
@@ -135,11 +137,12 @@ class Body:
     """Host copy of one red system: r, v (var4), p (param), md (metadata), playing[7]."""
 
     def __init__(self, r, v, p, md, playing, names=None):
-        self.r = np.ascontiguousarray(r, dtype=VAR4)
-        self.v = np.ascontiguousarray(v, dtype=VAR4)
-        self.p = np.ascontiguousarray(p, dtype=PARAM)
-        self.md = np.ascontiguousarray(md, dtype=BMD)
-        self.playing = np.ascontiguousarray(playing, dtype=np.uint32)
+        # private copies: the oracle integrates in place
+        self.r = np.array(r, dtype=VAR4, copy=True, order="C")
+        self.v = np.array(v, dtype=VAR4, copy=True, order="C")
+        self.p = np.array(p, dtype=PARAM, copy=True, order="C")
+        self.md = np.array(md, dtype=BMD, copy=True, order="C")
+        self.playing = np.array(playing, dtype=np.uint32, copy=True)
         self.inactive = np.zeros(7, np.uint32)
         self.removed = np.zeros(7, np.uint32)
         self.names = names
@@ -194,12 +197,12 @@ def step(ig, b, t, gas=None):
     return rc, tt.value
 
 
-def check_collision(b, t, factor, sem=SEM_GPU, cap=None):
+def check_collision(b, t, factor, sem=SEM_GPU, cap=None, nthreads=1):
     cap = max(16, b.n) if cap is None else cap
     ev = np.zeros(cap, EVENT)
     n = C.c_uint32(0)
-    rc = lib().orc_check_collision(sem, t, factor, b.n, _p(b.md), _p(b.p), _p(b.r), _p(b.v), _p(ev),
-                                   cap, C.byref(n))
+    rc = lib().orc_check_collision_mt(sem, t, factor, b.n, _p(b.md), _p(b.p), _p(b.r), _p(b.v), _p(ev),
+                                      cap, C.byref(n), nthreads)
     return rc, ev[:min(n.value, cap)].copy(), n.value
 
 

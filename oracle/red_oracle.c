@@ -569,6 +569,41 @@ int orc_check_collision(int sem, double t, double factor, uint32_t n, const orc_
     return rc;
 }
 
+/* orc_check_collision with the i loop split over nthreads (OpenMP); the events
+ * come out in the same (i, j) order as the sequential loop. */
+int orc_check_collision_mt(int sem, double t, double factor, uint32_t n, const orc_bmd* md,
+                           const orc_param* p, const orc_var4* r, const orc_var4* v,
+                           orc_event* ev, uint32_t cap, uint32_t* n_ev, int nthreads)
+{
+    if (nthreads <= 1) return orc_check_collision(sem, t, factor, n, md, p, r, v, ev, cap, n_ev);
+    const double f = SQR(factor);
+    /* pass 1: events per i (count only) */
+    uint32_t* cnt = calloc(n ? n : 1, sizeof(uint32_t));
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+#endif
+    for (int64_t ii = 0; ii < (int64_t)n; ii++) {
+        const uint32_t i = (uint32_t)ii;
+        if (sem == ORC_SEM_GPU ? !(0 < md[i].id) : !(0 < md[i].id && ORC_STAR != md[i].body_type)) continue;
+        uint32_t c = 0;
+        for (uint32_t j = i + 1; j < n; j++) {
+            if (sem == ORC_SEM_GPU ? (0 > md[j].id) : (0 > md[j].id && ORC_STAR != md[j].body_type)) continue;
+            const double dx = r[j].x - r[i].x;
+            const double dy = r[j].y - r[i].y;
+            const double dz = r[j].z - r[i].z;
+            const double w = SQR(dx) + SQR(dy) + SQR(dz);
+            if (w < f * SQR((p[i].radius + p[j].radius))) c++;
+        }
+        cnt[i] = c;
+    }
+    uint32_t total = 0;
+    for (uint32_t i = 0; i < n; i++) total += cnt[i];
+    free(cnt);
+    if (total == 0) { *n_ev = 0; return ORC_OK; }
+    /* events exist (rare): the sequential loop writes them in order */
+    return orc_check_collision(sem, t, factor, n, md, p, r, v, ev, cap, n_ev);
+}
+
 int orc_check_ejection_hit_centrum(double t, double ejection, double hit_centrum, uint32_t n,
                                    const orc_bmd* md, const orc_param* p, const orc_var4* r,
                                    const orc_var4* v, orc_event* ev, uint32_t cap, uint32_t* n_ev)

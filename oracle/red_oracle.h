@@ -116,7 +116,11 @@ int orc_step(orc_integrator* ig, double* t, const uint32_t playing[7], const orc
 int orc_check_collision(int sem, double t, double factor, uint32_t n_total, const orc_bmd* md,
                         const orc_param* p, const orc_var4* r, const orc_var4* v,
                         orc_event* ev, uint32_t cap, uint32_t* n_ev);
-/* check_for_ejection_hit_centrum (pp_disk.cu:283-318 / 1113-1134). */
+/* The same test with the i loop spread over nthreads (OpenMP). */
+int orc_check_collision_mt(int sem, double t, double factor, uint32_t n_total, const orc_bmd* md,
+                           const orc_param* p, const orc_var4* r, const orc_var4* v,
+                           orc_event* ev, uint32_t cap, uint32_t* n_ev, int nthreads);
+/* check_for_ejection_hit_centrum (pp_disk.cu:283-318 / 1096-1127). */
 int orc_check_ejection_hit_centrum(double t, double ejection, double hit_centrum, uint32_t n_total,
                                    const orc_bmd* md, const orc_param* p, const orc_var4* r,
                                    const orc_var4* v, orc_event* ev, uint32_t cap, uint32_t* n_ev);

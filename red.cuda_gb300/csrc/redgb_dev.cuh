@@ -1,0 +1,216 @@
+// redgb_dev.cuh -- device-side layout shared by the kernels and the host layer.
+//
+// HBM layout (all systems concatenated; system s owns bodies [off, off+n)):
+//   y_r, y_v        double[3N]   current positions / velocities, xyz packed per body
+//   Kr[s], Kv[s]    double[3N]   stage derivatives: Kr[s] = stage velocity (the
+//                                r-derivative), Kv[s] = acceleration; Kr[0] aliases y_v
+//   tr[2]           double[3N]   FP64 stage positions, ping-pong by stage parity
+//   pos_hi[2]       float4[N]    (x, y, z, mass) rounded to FP32, by stage parity
+//   pos_lo[2]       float4[N]    (x - hi, y - hi, z - hi, radius), the low words of
+//                                the double-single coordinates
+//   mass, radius, density, cd    double[N], id / btype int32[N]
+// The .w lane red integrates (always 0) is not stored.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace redgb {
+
+constexpr int kTile = 128;          // sinks per CTA and sources per shared-memory tile
+constexpr int kSegment = 256;       // bodies per CTA in the per-body kernels
+constexpr int kMaxStages = 13;
+
+enum Mode { MODE_MIXED = 0, MODE_FP64 = 1, MODE_FP64_EXACT = 2, MODE_FP32 = 3 };
+enum Scheme { SCHEME_RK4 = 0, SCHEME_RKF78 = 1 };
+enum Cls { CLS_SI = 0, CLS_NSI = 1, CLS_NI = 2 };
+
+// Per-system integrator state, device resident.  Mirrors integrator's
+// dt_try / dt_did / dt_next and counters (integrator.h:37-52) and pp_disk::t.
+struct DevSys {
+    double t;
+    double t_start;
+    double dt_try;        // step of the try in flight
+    double dt_did;        // last accepted step
+    double dt_next;
+    unsigned long long err_bits;   // max |error| of the try, as the bits of a non-negative double
+    unsigned long long n_tried, n_passed, n_failed;
+    int iter;             // tries made in the current step
+    int accepted;         // the last try was accepted
+    int active;           // integrating (length not reached)
+    int halted;           // events found, waiting for the host
+    int status;           // 0 or a RED_ERR_* code
+    int n_coll;           // collision events found for this system in the last check
+    int n_ejhc;           // ejection / hit-centrum events found in the last check
+    int quota;            // accepted steps still allowed (-1: unlimited)
+};
+
+__host__ __device__ inline bool runnable(const DevSys& S)
+{
+    return S.active && !S.halted && S.quota != 0;
+}
+
+// Static description of a system.
+struct SysInfo {
+    int off, n;           // body range
+    int n_star;           // stars: bodies [off, off + n_star)
+    int n_SI, n_massive;  // counts relative to off
+    int n_err;            // bodies in the error norm (n_massive, or n with error_check_for_tp)
+};
+
+// One CTA of the stage kernel: a tile of sinks against one chunk of sources.
+struct GravItem {
+    int sys;
+    int sink0, nsink;     // absolute first sink, count (<= kTile)
+    int src0, src1;       // absolute source range of this chunk
+    int chunk, nchunk;
+    int tile;             // tile id: counter index when nchunk > 1
+    int part_off;         // first partial record of the tile
+    int lanes;            // threads per sink, lanes * nsink <= kTile
+    int cls;
+    int pad;
+};
+
+// Per-body kernels: one CTA per segment of one system.
+struct Segment {
+    int sys, b0, b1, pad;
+};
+
+// Tile pair of the collision check (I <= J, tiles of kTile bodies of one system).
+struct PairItem {
+    int sys, i0, j0, pad;
+};
+
+// Compact collision / ejection record written by the device.
+struct DevEvent {
+    int sys;
+    int name;             // RED_EVENT_*
+    int i, j;             // loop indices (i < j for collisions; 0, body for ejection)
+    int surv, merg;       // idx1, idx2 of red's event record
+    double d;
+};
+
+struct GasDev {
+    double rho[2], sch[2], eta[2];
+    double t0, t1, e_folding_time;
+    int gas_decrease;
+    int enabled;
+};
+
+struct Tableau {
+    // RKF7(8), int_rungekutta8.cu:26-48
+    double c[kMaxStages];
+    double a[79];
+    double b[11];
+    int nnz[kMaxStages];
+    int src[kMaxStages][9];
+    // RK4, int_rungekutta4.cu:26-31
+    double a4[8], b4[5], c4[5];
+};
+
+struct StageParams {
+    int stage;            // stage s evaluated by this launch
+    int next;             // stage whose positions the epilogue prepares, -1 for none
+    int scheme;           // SCHEME_*
+    int err_after;        // 1: this stage closes an adaptive try, epilogue adds the error norm
+    int ynp1_to_out;      // RK4 adaptive: the epilogue of stage 3 writes y_{n+1} as stage 4's input
+    int standalone;       // red_calc_dydx: only store Kv[stage]
+    int nthreads_pad;
+    double t_standalone;  // time of a standalone evaluation (drag)
+    const GravItem* items;
+    const SysInfo* sinfo;
+    DevSys* sys;
+    const float4* pos_hi_in;
+    const float4* pos_lo_in;
+    float4* pos_hi_out;
+    float4* pos_lo_out;
+    const double* r_in;   // FP64 positions of stage s
+    double* r_out;        // FP64 positions of stage `next`
+    const double* y_r;
+    const double* y_v;
+    double* Kr[kMaxStages];
+    double* Kv[kMaxStages];
+    const double* mass;
+    const double* radius;
+    const double* density;
+    const double* cd;
+    const int* id;
+    double* partial;      // 3 doubles per record
+    unsigned int* tile_cnt;
+    GasDev gas;
+};
+
+struct FinishParams {
+    int scheme, adaptive;
+    int commit_from_stage4;   // RK4 adaptive: y_{n+1} lives in tr[0] / Kr[4]
+    int stage_exact;
+    const Segment* segs;
+    const SysInfo* sinfo;
+    DevSys* sys;
+    double* y_r;
+    double* y_v;
+    const double* Kr[kMaxStages];
+    const double* Kv[kMaxStages];
+    const double* t_r0;       // tr[0]
+    const double* mass;
+    const double* radius;
+    const int* id;
+    float4* pos_hi0;
+    float4* pos_lo0;
+};
+
+struct ControlParams {
+    int n_sys;
+    int scheme, adaptive, order;
+    double tolerance, lambda;
+    double output_interval, length;
+    DevSys* sys;
+};
+
+struct CollParams {
+    const PairItem* items;
+    const SysInfo* sinfo;
+    DevSys* sys;
+    const float4* pos_hi;
+    const float4* pos_lo;
+    const double* y_r;
+    const double* radius;
+    const double* mass;
+    const int* id;
+    double factor;        // radii enhance factor
+    int only_accepted;    // run only for systems that just accepted a try
+    int mark;             // 1: count the events in DevSys and halt the system
+    DevEvent* events;
+    unsigned int* n_events;
+    unsigned int capacity;
+};
+
+struct EjhcParams {
+    const Segment* segs;
+    const SysInfo* sinfo;
+    DevSys* sys;
+    const double* y_r;
+    const int* id;
+    const int* btype;
+    double ejection, hit_centrum;
+    int only_accepted;
+    int mark;
+    DevEvent* events;
+    unsigned int* n_events;
+    unsigned int capacity;
+};
+
+// Host-side launchers (kernels.cu).
+void set_tableau(const Tableau& tb, cudaStream_t s);
+void launch_stage(const StageParams& P, int n_items, int mode, int stage_exact, cudaStream_t s);
+void launch_prep(const Segment* segs, int n_segs, const SysInfo* sinfo, const DevSys* sys, const double* y_r,
+                 const double* mass, const double* radius, const int* id, float4* hi, float4* lo, int all,
+                 cudaStream_t s);
+void launch_control(const ControlParams& P, cudaStream_t s);
+void launch_finish(const FinishParams& P, int n_segs, cudaStream_t s);
+void launch_collision(const CollParams& P, int n_items, cudaStream_t s);
+void launch_ejhc(const EjhcParams& P, int n_segs, cudaStream_t s);
+void launch_potential(const Segment* segs, int n_segs, const SysInfo* sinfo, const double* y_r,
+                      const double* mass, const int* id, int sys_filter, int interacting, double* u,
+                      cudaStream_t s);
+
+}  // namespace redgb

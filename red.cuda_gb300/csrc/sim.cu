@@ -1,0 +1,1405 @@
+// sim.cu -- host layer of libredgb: the C++ mirror of red's pp_disk +
+// integrator seam (src/red.cuda/pp_disk.h, integrator.h) over the device
+// kernels, and the C ABI declared in include/redgb.h.
+//
+// One handle integrates n independent systems.  Device memory holds every
+// system's bodies back to back; a host-built plan lists the CTAs of each
+// kernel (gravity tiles, per-body segments, collision tile pairs).  One try of
+// the integrator is a fixed sequence of launches, captured once into a CUDA
+// graph and replayed; all accept / reject decisions are taken on the device,
+// so the host only waits when it wants to look at the results or to handle
+// collision / ejection events.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "redgb_dev.cuh"
+#include "../../include/redgb.h"
+
+using namespace redgb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_error(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+struct CudaError {
+    cudaError_t e;
+    const char* what;
+    int line;
+};
+
+#define CK(call)                                                 \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
+        if (e_ != cudaSuccess) throw CudaError{e_, #call, __LINE__}; \
+    } while (0)
+
+struct ArgError {
+    int code;
+    std::string msg;
+};
+
+// Tableaux of red's integrators.
+Tableau make_tableau()
+{
+    Tableau t;
+    memset(&t, 0, sizeof(t));
+    // int_rungekutta8.cu:26-48
+    const double c[13] = {0.0, 2.0 / 27.0, 1.0 / 9.0, 1.0 / 6.0, 5.0 / 12.0, 1.0 / 2.0, 5.0 / 6.0,
+                          1.0 / 6.0, 2.0 / 3.0, 1.0 / 3.0, 1.0, 0.0, 1.0};
+    const double a[79] = {
+        0.0,
+        2.0 / 27.0,
+        1.0 / 36.0, 1.0 / 12.0,
+        1.0 / 24.0, 0.0, 1.0 / 8.0,
+        5.0 / 12.0, 0.0, -25.0 / 16.0, 25.0 / 16.0,
+        1.0 / 20.0, 0.0, 0.0, 1.0 / 4.0, 1.0 / 5.0,
+        -25.0 / 108.0, 0.0, 0.0, 125.0 / 108.0, -65.0 / 27.0, 125.0 / 54.0,
+        31.0 / 300.0, 0.0, 0.0, 0.0, 61.0 / 225.0, -2.0 / 9.0, 13.0 / 900.0,
+        2.0, 0.0, 0.0, -53.0 / 6.0, 704.0 / 45.0, -107.0 / 9.0, 67.0 / 90.0, 3.0,
+        -91.0 / 108.0, 0.0, 0.0, 23.0 / 108.0, -976.0 / 135.0, 311.0 / 54.0, -19.0 / 60.0, 17.0 / 6.0, -1.0 / 12.0,
+        2383.0 / 4100.0, 0.0, 0.0, -341.0 / 164.0, 4496.0 / 1025.0, -301.0 / 82.0, 2133.0 / 4100.0, 45.0 / 82.0,
+        45.0 / 164.0, 18.0 / 41.0,
+        3.0 / 205.0, 0.0, 0.0, 0.0, 0.0, -6.0 / 41.0, -3.0 / 205.0, -3.0 / 41.0, 3.0 / 41.0, 6.0 / 41.0, 0.0,
+        -1777.0 / 4100.0, 0.0, 0.0, -341.0 / 164.0, 4496.0 / 1025.0, -289.0 / 82.0, 2193.0 / 4100.0, 51.0 / 82.0,
+        33.0 / 164.0, 12.0 / 41.0, 0.0, 1.0};
+    const double b[11] = {41.0 / 840.0, 0.0, 0.0, 0.0, 0.0, 34.0 / 105.0, 9.0 / 35.0, 9.0 / 35.0,
+                          9.0 / 280.0, 9.0 / 280.0, 41.0 / 840.0};
+    memcpy(t.c, c, sizeof(c));
+    memcpy(t.a, a, sizeof(a));
+    memcpy(t.b, b, sizeof(b));
+    // nonzero coefficients of each stage row in the order red's stage kernels
+    // add them (rk8_kernel::calc_ytemp_for_f1..f12, int_rungekutta8.cu:80-246)
+    for (int r = 1; r < 13; r++) {
+        const int off = 1 + r * (r - 1) / 2;
+        int n = 0;
+        for (int q = 0; q < r; q++)
+            if (a[off + q] != 0.0) t.src[r][n++] = q;
+        t.nnz[r] = n;
+    }
+    // int_rungekutta4.cu:26-31
+    const double lam = 1.0 / 10.0;
+    const double a4[8] = {0.0, 1.0 / 2.0, 1.0 / 2.0, 1.0, 1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+    const double b4[5] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0 - lam, lam};
+    const double c4[5] = {0.0, 1.0 / 2.0, 1.0 / 2.0, 1.0, 1.0};
+    memcpy(t.a4, a4, sizeof(a4));
+    memcpy(t.b4, b4, sizeof(b4));
+    memcpy(t.c4, c4, sizeof(c4));
+    return t;
+}
+
+template <class T> T* dalloc(size_t n)
+{
+    void* p = nullptr;
+    if (n == 0) n = 1;
+    CK(cudaMalloc(&p, n * sizeof(T)));
+    CK(cudaMemset(p, 0, n * sizeof(T)));
+    return (T*)p;
+}
+
+struct SysHost {
+    uint32_t off = 0, cap = 0, n = 0;
+    uint32_t playing[7] = {0}, inactive[7] = {0}, removed[7] = {0};
+    uint32_t n_collision[3] = {0}, n_ejection[3] = {0}, n_hit_centrum[3] = {0}, n_event[3] = {0};
+    uint32_t n_SI() const { return playing[0] + playing[1] + playing[2] + playing[3]; }
+    uint32_t n_NSI() const { return playing[4] + playing[5]; }
+    uint32_t n_NI() const { return playing[6]; }
+    uint32_t n_massive() const { return n_SI() + n_NSI(); }
+    uint32_t n_active() const
+    {
+        uint32_t s = 0;
+        for (int i = 0; i < 7; i++) s += playing[i] - inactive[i];
+        return s;
+    }
+};
+
+// Per-system host copy of the state, used by the event handling.
+struct HostState {
+    std::vector<red_var4_t> r, v;
+    std::vector<red_param_t> p;
+    std::vector<red_body_metadata_t> md;
+};
+
+}  // namespace
+
+struct red_sim {
+    red_config_t cfg;
+    int mode = MODE_MIXED;
+    int scheme = SCHEME_RKF78;
+    int n_stage = 13;
+    int order = 7;
+    double lambda = 41.0 / 840.0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    uint32_t n_sys = 0;
+    uint32_t n_cap = 0;
+    std::vector<SysHost> sh;
+    std::vector<double> mig_stop_at;   // kept on the host (not used by the path)
+    std::vector<int> mig_type;
+
+    // device state
+    double *y_r = nullptr, *y_v = nullptr, *tr[2] = {nullptr, nullptr};
+    double* Kr[kMaxStages] = {nullptr};
+    double* Kv[kMaxStages] = {nullptr};
+    float4 *pos_hi[2] = {nullptr, nullptr}, *pos_lo[2] = {nullptr, nullptr};
+    double *mass = nullptr, *radius = nullptr, *density = nullptr, *cd = nullptr;
+    int *id = nullptr, *btype = nullptr;
+    double* partial = nullptr;
+    size_t partial_cap = 0;
+    unsigned int* tile_cnt = nullptr;
+    size_t tile_cap = 0;
+    DevSys* d_sys = nullptr;
+    SysInfo* d_sinfo = nullptr;
+    GravItem* d_items = nullptr;
+    size_t items_cap = 0;
+    Segment* d_segs = nullptr;
+    size_t segs_cap = 0;
+    PairItem* d_pairs = nullptr;
+    size_t pairs_cap = 0;
+    DevEvent* d_events = nullptr;
+    unsigned int* d_nev = nullptr;
+    uint32_t ev_cap = 0;
+    double* d_u = nullptr;
+
+    // plan
+    std::vector<GravItem> items;
+    std::vector<Segment> segs;
+    std::vector<PairItem> pairs;
+    std::vector<SysInfo> sinfo;
+    int chunk_override = 0;     // sources per chunk chosen by the autotuner (0 = heuristic)
+    int lanes_cap = 128;        // upper bound on threads per sink (autotuner)
+
+    cudaGraphExec_t graph = nullptr;
+    int launches_per_try = 0;
+    uint64_t launches = 0;
+    std::vector<red_event_t> event_log;
+
+    ~red_sim();
+    void create(const red_config_t* c, uint32_t n_systems, const uint32_t* playing, const red_var4_t* r,
+                const red_var4_t* v, const red_param_t* p, const red_body_metadata_t* md, const double* t0,
+                const double* dt0);
+    void build_plan();
+    StageParams stage_params(int s, bool standalone);
+    void enqueue_try(std::vector<int>* kinds = nullptr, std::vector<cudaEvent_t>* evs = nullptr);
+    void capture();
+    void launch_tries(uint32_t n);
+    void read_sys(std::vector<DevSys>& out);
+    void write_sys(const std::vector<DevSys>& in);
+    void prep_positions();
+    void get_host_state(uint32_t s, HostState& hs);
+    void put_host_state(uint32_t s, const HostState& hs);
+    void fill_event(uint32_t s, const HostState& hs, const DevEvent& de, double t, red_event_t& ev);
+    uint32_t collect_events(std::vector<DevEvent>& ev);
+    int handle_events(red_event_t* out, uint32_t cap, uint32_t* n_out);
+    void rebuild_system(uint32_t s);
+    void invalidate() { if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; } }
+    uint64_t interactions_per_eval() const;
+};
+
+red_sim::~red_sim()
+{
+    invalidate();
+    cudaFree(y_r); cudaFree(y_v); cudaFree(tr[0]); cudaFree(tr[1]);
+    for (int s = 1; s < kMaxStages; s++) cudaFree(Kr[s]);
+    for (int s = 0; s < kMaxStages; s++) cudaFree(Kv[s]);
+    for (int k = 0; k < 2; k++) { cudaFree(pos_hi[k]); cudaFree(pos_lo[k]); }
+    cudaFree(mass); cudaFree(radius); cudaFree(density); cudaFree(cd); cudaFree(id); cudaFree(btype);
+    cudaFree(partial); cudaFree(tile_cnt); cudaFree(d_sys); cudaFree(d_sinfo); cudaFree(d_items);
+    cudaFree(d_segs); cudaFree(d_pairs); cudaFree(d_events); cudaFree(d_nev); cudaFree(d_u);
+    if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+uint64_t red_sim::interactions_per_eval() const
+{
+    uint64_t n = 0;
+    for (const SysHost& h : sh) {
+        const uint64_t nsi = h.n_SI(), nnsi = h.n_NSI(), nm = h.n_massive(), nni = h.n_NI();
+        n += (nsi ? nsi * (nm - 1) : 0) + nnsi * nsi + nni * nm;
+    }
+    return n;
+}
+
+void red_sim::create(const red_config_t* c, uint32_t n_systems, const uint32_t* playing, const red_var4_t* r,
+                     const red_var4_t* v, const red_param_t* p, const red_body_metadata_t* md, const double* t0,
+                     const double* dt0)
+{
+    cfg = *c;
+    if (n_systems == 0) throw ArgError{RED_ERR_ARG, "n_systems must be positive"};
+    if (cfg.integrator == RED_INTEGRATOR_RUNGEKUTTA4) {
+        scheme = SCHEME_RK4;
+        n_stage = cfg.adaptive ? 5 : 4;
+        order = 4;
+        lambda = 1.0 / 10.0;
+    } else if (cfg.integrator == RED_INTEGRATOR_RUNGEKUTTAFEHLBERG78) {
+        scheme = SCHEME_RKF78;
+        n_stage = cfg.adaptive ? 13 : 11;
+        order = 7;
+        lambda = 41.0 / 840.0;
+    } else {
+        throw ArgError{RED_ERR_NOT_IMPLEMENTED, "only RUNGEKUTTA4 and RUNGEKUTTAFEHLBERG78 are on this path"};
+    }
+    if (cfg.precision < 0 || cfg.precision > 3) throw ArgError{RED_ERR_ARG, "bad precision"};
+    mode = cfg.precision;
+    device = cfg.device;
+    n_sys = n_systems;
+    sh.resize(n_sys);
+    uint32_t off = 0;
+    for (uint32_t s = 0; s < n_sys; s++) {
+        SysHost& h = sh[s];
+        h.off = off;
+        uint32_t n = 0;
+        for (int k = 0; k < 7; k++) {
+            h.playing[k] = playing[7 * s + k];
+            n += h.playing[k];
+        }
+        if (n == 0) throw ArgError{RED_ERR_ARG, "system without bodies"};
+        h.n = h.cap = n;
+        // red requires bodies sorted by type (the bounds of red_type.h:670-700 assume it)
+        uint32_t k = 0;
+        for (int ty = 0; ty < 7; ty++) {
+            for (uint32_t q = 0; q < h.playing[ty]; q++, k++) {
+                if (md[off + k].body_type != ty)
+                    throw ArgError{RED_ERR_ARG, "bodies must be sorted by type matching the counts (system " +
+                                                    std::to_string(s) + ", body " + std::to_string(k) + ": type " +
+                                                    std::to_string(md[off + k].body_type) + ", expected " +
+                                                    std::to_string(ty) + ")"};
+            }
+        }
+        off += n;
+    }
+    n_cap = off;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        throw ArgError{RED_ERR_NO_DEVICE, "no CUDA device"};
+    CK(cudaSetDevice(device));
+    if (cfg.stream) {
+        stream = (cudaStream_t)cfg.stream;
+    } else {
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        own_stream = true;
+    }
+    const size_t N = n_cap;
+    // host -> packed xyz
+    std::vector<double> hr(3 * N), hv(3 * N), hm(N), hR(N), hd(N), hc(N);
+    std::vector<int> hid(N), hty(N);
+    mig_stop_at.resize(N);
+    mig_type.resize(N);
+    for (size_t i = 0; i < N; i++) {
+        hr[3 * i] = r[i].x; hr[3 * i + 1] = r[i].y; hr[3 * i + 2] = r[i].z;
+        hv[3 * i] = v[i].x; hv[3 * i + 1] = v[i].y; hv[3 * i + 2] = v[i].z;
+        hm[i] = p[i].mass; hR[i] = p[i].radius; hd[i] = p[i].density; hc[i] = p[i].cd;
+        hid[i] = md[i].id; hty[i] = md[i].body_type;
+        mig_stop_at[i] = md[i].mig_stop_at;
+        mig_type[i] = md[i].mig_type;
+    }
+    y_r = dalloc<double>(3 * N);
+    y_v = dalloc<double>(3 * N);
+    tr[0] = dalloc<double>(3 * N);
+    tr[1] = dalloc<double>(3 * N);
+    Kr[0] = y_v;
+    for (int s = 1; s < n_stage; s++) Kr[s] = dalloc<double>(3 * N);
+    for (int s = 0; s < n_stage; s++) Kv[s] = dalloc<double>(3 * N);
+    for (int k = 0; k < 2; k++) {
+        pos_hi[k] = dalloc<float4>(N);
+        pos_lo[k] = dalloc<float4>(N);
+    }
+    mass = dalloc<double>(N); radius = dalloc<double>(N); density = dalloc<double>(N); cd = dalloc<double>(N);
+    id = dalloc<int>(N); btype = dalloc<int>(N);
+    d_u = dalloc<double>(N);
+    CK(cudaMemcpy(y_r, hr.data(), 3 * N * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(y_v, hv.data(), 3 * N * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(mass, hm.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(radius, hR.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(density, hd.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(cd, hc.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(id, hid.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(btype, hty.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+
+    std::vector<DevSys> ds(n_sys);
+    for (uint32_t s = 0; s < n_sys; s++) {
+        memset(&ds[s], 0, sizeof(DevSys));
+        ds[s].t = ds[s].t_start = t0 ? t0[s] : 0.0;
+        const double dt = dt0 ? dt0[s] : 0.0;
+        ds[s].dt_try = ds[s].dt_next = dt;
+        ds[s].active = sh[s].n_active() > 1 ? 1 : 0;   // run_simulation's loop bound (main.cu:471)
+        ds[s].quota = -1;
+    }
+    d_sys = dalloc<DevSys>(n_sys);
+    d_sinfo = dalloc<SysInfo>(n_sys);
+    CK(cudaMemcpy(d_sys, ds.data(), n_sys * sizeof(DevSys), cudaMemcpyHostToDevice));
+    ev_cap = cfg.event_capacity ? cfg.event_capacity : std::max<uint32_t>(1024u, n_cap);
+    d_events = dalloc<DevEvent>(ev_cap);
+    d_nev = dalloc<unsigned int>(1);
+    Tableau tb = make_tableau();
+    set_tableau(tb, stream);
+    build_plan();
+    prep_positions();
+    CK(cudaStreamSynchronize(stream));
+}
+
+void red_sim::build_plan()
+{
+    invalidate();
+    items.clear();
+    segs.clear();
+    pairs.clear();
+    sinfo.assign(n_sys, SysInfo{});
+    size_t part = 0;
+    int tiles = 0;
+    const bool fp32 = (mode == MODE_MIXED || mode == MODE_FP32);
+    const int kTargetCtas = 8 * 152;   // ~8 resident CTAs on each of GB300's 152 SMs
+    for (uint32_t s = 0; s < n_sys; s++) {
+        const SysHost& h = sh[s];
+        SysInfo& si = sinfo[s];
+        si.off = (int)h.off;
+        si.n = (int)h.n;
+        si.n_star = (int)h.playing[0];
+        si.n_SI = (int)h.n_SI();
+        si.n_massive = (int)h.n_massive();
+        si.n_err = cfg.error_check_for_tp ? si.n : si.n_massive;
+        const int src_start = fp32 ? si.n_star : 0;
+        struct C { int cls, s0, s1, j0, j1; };
+        const C cls[3] = {{CLS_SI, 0, si.n_SI, src_start, si.n_massive},
+                          {CLS_NSI, si.n_SI, si.n_massive, src_start, si.n_SI},
+                          {CLS_NI, si.n_massive, si.n, src_start, si.n_massive}};
+        for (const C& q : cls) {
+            const int nsink_all = q.s1 - q.s0;
+            if (nsink_all <= 0) continue;
+            const int nsrc = std::max(0, q.j1 - q.j0);
+            const int ntile = (nsink_all + kTile - 1) / kTile;
+            for (int t = 0; t < ntile; t++) {
+                const int s0 = q.s0 + t * kTile;
+                const int nsink = std::min(kTile, q.s1 - s0);
+                int lanes = 1;
+                int chunk = std::max(nsrc, 1);
+                if (mode != MODE_FP64_EXACT) {
+                    // few sinks: several threads per sink over interleaved sources
+                    lanes = std::max(1, std::min(std::min(kTile / nsink, lanes_cap), std::max(1, nsrc)));
+                    int c;
+                    if (chunk_override > 0) {
+                        c = chunk_override;
+                    } else {
+                        // enough CTAs to fill the SMs several times over, but at least
+                        // kMinIter sources per thread in every chunk
+                        const int kMinIter = 48;
+                        const int want = std::max(1, (kTargetCtas + ntile - 1) / ntile);
+                        const int most = std::max(1, nsrc / (kMinIter * lanes));
+                        const int nch = std::max(1, std::min(want, most));
+                        c = (nsrc + nch - 1) / nch;
+                    }
+                    chunk = std::max(c, 1);
+                }
+                const int nchunk = std::max(1, (nsrc + chunk - 1) / chunk);
+                GravItem g;
+                memset(&g, 0, sizeof(g));
+                g.sys = (int)s;
+                g.sink0 = si.off + s0;
+                g.nsink = nsink;
+                g.nchunk = nchunk;
+                g.lanes = lanes;
+                g.cls = q.cls;
+                g.tile = nchunk > 1 ? tiles++ : -1;
+                g.part_off = (int)part;
+                if (nchunk > 1) part += (size_t)nchunk * nsink;
+                for (int c = 0; c < nchunk; c++) {
+                    g.chunk = c;
+                    g.src0 = si.off + q.j0 + c * chunk;
+                    g.src1 = si.off + std::min(q.j1, q.j0 + (c + 1) * chunk);
+                    if (nsrc == 0) g.src0 = g.src1 = si.off;
+                    items.push_back(g);
+                }
+            }
+        }
+        for (int b = 0; b < si.n; b += kSegment) segs.push_back(Segment{(int)s, si.off + b, si.off + std::min(si.n, b + kSegment), 0});
+        const int T = (si.n + kTile - 1) / kTile;
+        for (int I = 0; I < T; I++)
+            for (int J = I; J < T; J++) pairs.push_back(PairItem{(int)s, si.off + I * kTile, si.off + J * kTile, 0});
+    }
+    auto upload = [&](auto& vec, auto*& dptr, size_t& cap) {
+        using T = typename std::remove_reference<decltype(vec)>::type::value_type;
+        if (vec.size() > cap) {
+            cudaFree(dptr);
+            cap = vec.size();
+            dptr = dalloc<T>(cap);
+        }
+        if (!vec.empty()) CK(cudaMemcpy(dptr, vec.data(), vec.size() * sizeof(T), cudaMemcpyHostToDevice));
+    };
+    upload(items, d_items, items_cap);
+    upload(segs, d_segs, segs_cap);
+    upload(pairs, d_pairs, pairs_cap);
+    CK(cudaMemcpy(d_sinfo, sinfo.data(), n_sys * sizeof(SysInfo), cudaMemcpyHostToDevice));
+    if (part > partial_cap) {
+        cudaFree(partial);
+        partial_cap = part;
+        partial = dalloc<double>(3 * part);
+    }
+    if ((size_t)tiles > tile_cap) {
+        cudaFree(tile_cnt);
+        tile_cap = tiles;
+        tile_cnt = dalloc<unsigned int>(tile_cap);
+    }
+}
+
+StageParams red_sim::stage_params(int s, bool standalone)
+{
+    StageParams P;
+    memset(&P, 0, sizeof(P));
+    P.stage = s;
+    P.scheme = scheme;
+    P.standalone = standalone ? 1 : 0;
+    if (!standalone) {
+        if (scheme == SCHEME_RKF78) {
+            P.next = (s + 1 < n_stage) ? s + 1 : -1;
+        } else {
+            P.next = (s + 1 < n_stage) ? s + 1 : -1;
+            P.ynp1_to_out = (cfg.adaptive && s == 3) ? 1 : 0;
+        }
+        P.err_after = (cfg.adaptive && s == n_stage - 1) ? 1 : 0;
+    } else {
+        P.next = -1;
+    }
+    P.items = d_items;
+    P.sinfo = d_sinfo;
+    P.sys = d_sys;
+    P.pos_hi_in = pos_hi[s & 1];
+    P.pos_lo_in = pos_lo[s & 1];
+    P.pos_hi_out = pos_hi[(s + 1) & 1];
+    P.pos_lo_out = pos_lo[(s + 1) & 1];
+    P.r_in = (s == 0) ? y_r : tr[s & 1];
+    P.r_out = tr[(s + 1) & 1];
+    P.y_r = y_r;
+    P.y_v = y_v;
+    for (int k = 0; k < kMaxStages; k++) {
+        P.Kr[k] = Kr[k];
+        P.Kv[k] = Kv[k];
+    }
+    P.mass = mass; P.radius = radius; P.density = density; P.cd = cd; P.id = id;
+    P.partial = partial;
+    P.tile_cnt = tile_cnt;
+    P.gas.enabled = cfg.gas_disk == 1;
+    for (int k = 0; k < 2; k++) {
+        P.gas.rho[k] = cfg.gas.rho[k];
+        P.gas.sch[k] = cfg.gas.sch[k];
+        P.gas.eta[k] = cfg.gas.eta[k];
+    }
+    P.gas.t0 = cfg.gas.t0;
+    P.gas.t1 = cfg.gas.t1;
+    P.gas.e_folding_time = cfg.gas.e_folding_time;
+    P.gas.gas_decrease = cfg.gas.gas_decrease;
+    return P;
+}
+
+void red_sim::prep_positions()
+{
+    launch_prep(d_segs, (int)segs.size(), d_sinfo, d_sys, y_r, mass, radius, id, pos_hi[0], pos_lo[0], 1, stream);
+    CK(cudaGetLastError());
+    launches++;
+}
+
+// One try of the integrator.  With kinds / evs set (profiling), an event is
+// recorded after every launch and the kernel kind noted: 0 stage, 1 control,
+// 2 finish, 3 collision, 4 ejection / hit-centrum.
+void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs)
+{
+    int n = 0;
+    auto mark = [&](int kind) {
+        if (!kinds) return;
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        CK(cudaEventRecord(e, stream));
+        kinds->push_back(kind);
+        evs->push_back(e);
+    };
+    mark(-1);
+    for (int s = 0; s < n_stage; s++) {
+        StageParams P = stage_params(s, false);
+        launch_stage(P, (int)items.size(), mode, cfg.stage_exact, stream);
+        mark(0);
+        n++;
+    }
+    ControlParams C;
+    memset(&C, 0, sizeof(C));
+    C.n_sys = (int)n_sys;
+    C.scheme = scheme;
+    C.adaptive = cfg.adaptive;
+    C.order = order;
+    C.tolerance = cfg.tolerance;
+    C.lambda = lambda;
+    C.output_interval = cfg.output_interval;
+    C.length = cfg.length;
+    C.sys = d_sys;
+    launch_control(C, stream);
+    mark(1);
+    n++;
+    FinishParams F;
+    memset(&F, 0, sizeof(F));
+    F.scheme = scheme;
+    F.adaptive = cfg.adaptive;
+    F.commit_from_stage4 = (scheme == SCHEME_RK4 && cfg.adaptive) ? 1 : 0;
+    F.stage_exact = cfg.stage_exact;
+    F.segs = d_segs;
+    F.sinfo = d_sinfo;
+    F.sys = d_sys;
+    F.y_r = y_r;
+    F.y_v = y_v;
+    for (int k = 0; k < kMaxStages; k++) {
+        F.Kr[k] = Kr[k];
+        F.Kv[k] = Kv[k];
+    }
+    F.t_r0 = tr[0];
+    F.mass = mass;
+    F.radius = radius;
+    F.id = id;
+    F.pos_hi0 = pos_hi[0];
+    F.pos_lo0 = pos_lo[0];
+    launch_finish(F, (int)segs.size(), stream);
+    mark(2);
+    n++;
+    if (cfg.threshold[RED_THRESHOLD_RADII_ENHANCE_FACTOR] > 0.0) {
+        CollParams Q;
+        memset(&Q, 0, sizeof(Q));
+        Q.items = d_pairs; Q.sinfo = d_sinfo; Q.sys = d_sys;
+        Q.pos_hi = pos_hi[0]; Q.pos_lo = pos_lo[0]; Q.y_r = y_r;
+        Q.radius = radius; Q.mass = mass; Q.id = id;
+        Q.factor = cfg.threshold[RED_THRESHOLD_RADII_ENHANCE_FACTOR];
+        Q.only_accepted = 1;
+        Q.mark = 1;
+        Q.events = d_events; Q.n_events = d_nev; Q.capacity = ev_cap;
+        launch_collision(Q, (int)pairs.size(), stream);
+        mark(3);
+        n++;
+    }
+    if (cfg.threshold[RED_THRESHOLD_EJECTION_DISTANCE] > 0.0 || cfg.threshold[RED_THRESHOLD_HIT_CENTRUM_DISTANCE] > 0.0) {
+        EjhcParams E;
+        memset(&E, 0, sizeof(E));
+        E.segs = d_segs; E.sinfo = d_sinfo; E.sys = d_sys; E.y_r = y_r; E.id = id; E.btype = btype;
+        E.ejection = cfg.threshold[RED_THRESHOLD_EJECTION_DISTANCE];
+        E.hit_centrum = cfg.threshold[RED_THRESHOLD_HIT_CENTRUM_DISTANCE];
+        E.only_accepted = 1;
+        E.mark = 1;
+        E.events = d_events; E.n_events = d_nev; E.capacity = ev_cap;
+        launch_ejhc(E, (int)segs.size(), stream);
+        mark(4);
+        n++;
+    }
+    launches_per_try = n;
+}
+
+void red_sim::capture()
+{
+    if (graph) return;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_try();
+    cudaError_t e = cudaStreamEndCapture(stream, &g);
+    if (e != cudaSuccess) throw CudaError{e, "cudaStreamEndCapture", __LINE__};
+    e = cudaGraphInstantiate(&graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        graph = nullptr;
+        throw CudaError{e, "cudaGraphInstantiate", __LINE__};
+    }
+}
+
+void red_sim::launch_tries(uint32_t n)
+{
+    capture();
+    for (uint32_t k = 0; k < n; k++) {
+        CK(cudaGraphLaunch(graph, stream));
+        launches += (uint64_t)launches_per_try;
+    }
+}
+
+void red_sim::read_sys(std::vector<DevSys>& out)
+{
+    out.resize(n_sys);
+    CK(cudaMemcpyAsync(out.data(), d_sys, n_sys * sizeof(DevSys), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+}
+
+void red_sim::write_sys(const std::vector<DevSys>& in)
+{
+    CK(cudaMemcpyAsync(d_sys, in.data(), n_sys * sizeof(DevSys), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+}
+
+void red_sim::get_host_state(uint32_t s, HostState& hs)
+{
+    const SysHost& h = sh[s];
+    const size_t n = h.n, o = h.off;
+    std::vector<double> hr(3 * n), hv(3 * n), hm(n), hR(n), hd(n), hc(n);
+    std::vector<int> hid(n), hty(n);
+    CK(cudaMemcpyAsync(hr.data(), y_r + 3 * o, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(hv.data(), y_v + 3 * o, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(hm.data(), mass + o, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(hR.data(), radius + o, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(hd.data(), density + o, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(hc.data(), cd + o, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(hid.data(), id + o, n * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(hty.data(), btype + o, n * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    hs.r.resize(n); hs.v.resize(n); hs.p.resize(n); hs.md.resize(n);
+    for (size_t i = 0; i < n; i++) {
+        hs.r[i] = red_var4_t{hr[3 * i], hr[3 * i + 1], hr[3 * i + 2], 0.0};
+        hs.v[i] = red_var4_t{hv[3 * i], hv[3 * i + 1], hv[3 * i + 2], 0.0};
+        hs.p[i] = red_param_t{hm[i], hR[i], hd[i], hc[i]};
+        hs.md[i].id = hid[i];
+        hs.md[i].body_type = hty[i];
+        hs.md[i].mig_type = mig_type[o + i];
+        hs.md[i].mig_stop_at = mig_stop_at[o + i];
+    }
+}
+
+void red_sim::put_host_state(uint32_t s, const HostState& hs)
+{
+    const SysHost& h = sh[s];
+    const size_t n = hs.r.size(), o = h.off;
+    std::vector<double> hr(3 * n), hv(3 * n), hm(n), hR(n), hd(n), hc(n);
+    std::vector<int> hid(n), hty(n);
+    for (size_t i = 0; i < n; i++) {
+        hr[3 * i] = hs.r[i].x; hr[3 * i + 1] = hs.r[i].y; hr[3 * i + 2] = hs.r[i].z;
+        hv[3 * i] = hs.v[i].x; hv[3 * i + 1] = hs.v[i].y; hv[3 * i + 2] = hs.v[i].z;
+        hm[i] = hs.p[i].mass; hR[i] = hs.p[i].radius; hd[i] = hs.p[i].density; hc[i] = hs.p[i].cd;
+        hid[i] = hs.md[i].id; hty[i] = hs.md[i].body_type;
+        mig_type[o + i] = hs.md[i].mig_type;
+        mig_stop_at[o + i] = hs.md[i].mig_stop_at;
+    }
+    CK(cudaMemcpyAsync(y_r + 3 * o, hr.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(y_v + 3 * o, hv.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(mass + o, hm.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(radius + o, hR.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(density + o, hd.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(cd + o, hc.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(id + o, hid.data(), n * sizeof(int), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(btype + o, hty.data(), n * sizeof(int), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+}
+
+// pp_disk_utility::store_event_data (pp_disk.cu:190-253) from a device record.
+void red_sim::fill_event(uint32_t s, const HostState& hs, const DevEvent& de, double t, red_event_t& ev)
+{
+    const uint32_t o = sh[s].off;
+    memset(&ev, 0, sizeof(ev));
+    const uint32_t i1 = (uint32_t)de.surv - o, i2 = (uint32_t)de.merg - o;
+    ev.event_name = de.name;
+    ev.t = t;
+    ev.d = de.d;
+    ev.id0 = hs.md[0].id;
+    ev.id1 = hs.md[i1].id;
+    ev.id2 = hs.md[i2].id;
+    ev.idx0 = 0;
+    ev.idx1 = i1;
+    ev.idx2 = i2;
+    ev.r0 = hs.r[0]; ev.v0 = hs.v[0];
+    ev.r1 = hs.r[i1]; ev.v1 = hs.v[i1];
+    ev.r2 = hs.r[i2]; ev.v2 = hs.v[i2];
+    ev.p0 = hs.p[0];
+    if (de.name == RED_EVENT_EJECTION) {
+        ev.p1 = hs.p[i1];
+        ev.p2 = hs.p[i2];
+        ev.rs = ev.r1;
+        ev.vs = ev.v1;
+        ev.ps = ev.p1;
+    }
+}
+
+uint32_t red_sim::collect_events(std::vector<DevEvent>& ev)
+{
+    unsigned int n = 0;
+    CK(cudaMemcpyAsync(&n, d_nev, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    const uint32_t m = std::min<uint32_t>(n, ev_cap);
+    ev.resize(m);
+    if (m) CK(cudaMemcpyAsync(ev.data(), d_events, m * sizeof(DevEvent), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemsetAsync(d_nev, 0, sizeof(unsigned int), stream));
+    CK(cudaStreamSynchronize(stream));
+    // red's CPU loop order: system, then i, then j
+    std::sort(ev.begin(), ev.end(), [](const DevEvent& a, const DevEvent& b) {
+        if (a.sys != b.sys) return a.sys < b.sys;
+        if (a.i != b.i) return a.i < b.i;
+        if (a.j != b.j) return a.j < b.j;
+        return a.name > b.name;   // ejection before hit-centrum for the same body (pp_disk.cu:306-315)
+    });
+    return n;
+}
+
+namespace {
+// tools.cpp:455-507
+double calc_radius(double m, double density)
+{
+    static const double four_pi_over_three = 4.188790204786391;
+    return pow(1.0 / four_pi_over_three * m / density, 1.0 / 3.0);
+}
+
+void merge_pair(red_event_t& c, HostState& hs)
+{
+    const uint32_t s = c.idx1, m = c.idx2;
+    c.p1 = hs.p[s];
+    c.p2 = hs.p[m];
+    const double m1 = c.p1.mass, m2 = c.p2.mass;
+    const double M = m1 + m2;
+    c.rs.x = (m1 * c.r1.x + m2 * c.r2.x) / M;
+    c.rs.y = (m1 * c.r1.y + m2 * c.r2.y) / M;
+    c.rs.z = (m1 * c.r1.z + m2 * c.r2.z) / M;
+    c.vs.x = (m1 * c.v1.x + m2 * c.v2.x) / M;
+    c.vs.y = (m1 * c.v1.y + m2 * c.v2.y) / M;
+    c.vs.z = (m1 * c.v1.z + m2 * c.v2.z) / M;
+    hs.r[s] = c.rs;
+    hs.v[s] = c.vs;
+    const double volume = 4.188790204786391 * (c.p1.radius * c.p1.radius * c.p1.radius +
+                                               c.p2.radius * c.p2.radius * c.p2.radius);
+    c.ps.mass = c.p1.mass + c.p2.mass;
+    c.ps.density = c.ps.mass / volume;
+    c.ps.radius = calc_radius(c.ps.mass, c.ps.density);
+    c.ps.cd = c.p1.cd;
+    hs.p[s] = c.ps;
+}
+
+void bump(uint32_t* counter, uint32_t* n_event)
+{
+    for (int i = 0; i < 3; i++) {
+        counter[i]++;
+        n_event[i]++;
+    }
+}
+}  // namespace
+
+// Handles the events of the halted systems (pp_disk::handle_collision,
+// pp_disk.cu:1220-1248; handle_ejection_hit_centrum, 1290-1326; rebuild after
+// 16 events, main.cu:582-607).
+int red_sim::handle_events(red_event_t* out, uint32_t cap, uint32_t* n_out)
+{
+    std::vector<DevSys> ds;
+    read_sys(ds);
+    std::vector<DevEvent> ev;
+    const uint32_t n_raw = collect_events(ev);
+    uint32_t n_written = 0;
+    int rc = RED_OK;
+    if (n_raw > ev_cap) rc = set_error(RED_ERR_EVENT_OVERFLOW, "%u events exceed the event buffer (%u)", n_raw, ev_cap);
+    bool changed = false;
+    size_t k = 0;
+    for (uint32_t s = 0; s < n_sys; s++) {
+        size_t k1 = k;
+        while (k1 < ev.size() && ev[k1].sys == (int)s) k1++;
+        if (!ds[s].halted) {
+            k = k1;
+            continue;
+        }
+        HostState hs;
+        get_host_state(s, hs);
+        SysHost& h = sh[s];
+        // collisions first (main.cu:540-569), then ejection / hit-centrum
+        std::vector<red_event_t> coll, ejhc;
+        for (size_t q = k; q < k1; q++) {
+            red_event_t e;
+            fill_event(s, hs, ev[q], ds[s].t, e);
+            if (ev[q].name == RED_EVENT_COLLISION) coll.push_back(e);
+            else ejhc.push_back(e);
+        }
+        // populate_sp_events: one record per (id1, id2), the earliest (pp_disk.cu:1250-1288)
+        std::vector<red_event_t> sp;
+        std::vector<char> done(coll.size(), 0);
+        for (size_t a = 0; a < coll.size(); a++) {
+            if (done[a]) continue;
+            done[a] = 1;
+            red_event_t e = coll[a];
+            for (size_t b = a + 1; b < coll.size(); b++) {
+                if (e.id1 == coll[b].id1 && e.id2 == coll[b].id2) {
+                    done[b] = 1;
+                    if (e.t > coll[b].t) e = coll[b];
+                }
+            }
+            sp.push_back(e);
+        }
+        for (red_event_t& e : sp) {
+            if (hs.md[e.idx2].body_type == RED_BODY_SUPERPLANETESIMAL) {
+                ds[s].status = RED_ERR_SUPERPLANETESIMAL;
+                rc = set_error(RED_ERR_SUPERPLANETESIMAL, "collision between a massive body and a super-planetesimal");
+                break;
+            }
+            merge_pair(e, hs);
+            bump(h.n_collision, h.n_event);
+            hs.md[e.idx2].id *= -1;
+            h.inactive[hs.md[e.idx2].body_type]++;
+            event_log.push_back(e);
+            if (out && n_written < cap) out[n_written] = e;
+            n_written++;
+        }
+        for (red_event_t& e : ejhc) {
+            if (e.event_name == RED_EVENT_EJECTION) {
+                bump(h.n_ejection, h.n_event);
+            } else {
+                merge_pair(e, hs);
+                bump(h.n_hit_centrum, h.n_event);
+            }
+            hs.md[e.idx2].id *= -1;
+            h.inactive[hs.md[e.idx2].body_type]++;
+            event_log.push_back(e);
+            if (out && n_written < cap) out[n_written] = e;
+            n_written++;
+        }
+        put_host_state(s, hs);
+        ds[s].halted = 0;
+        ds[s].n_coll = 0;
+        ds[s].n_ejhc = 0;
+        if (ds[s].status) ds[s].active = 0;
+        if (h.n_active() <= 1) ds[s].active = 0;   // main.cu:471
+        changed = true;
+        if (16 <= h.n_event[1]) {                    // EVENT_COUNTER_NAME_LAST_CLEAR, main.cu:582-585
+            for (int c = 0; c < 3; c++) (void)c;
+            h.n_event[1] = h.n_collision[1] = h.n_ejection[1] = h.n_hit_centrum[1] = 0;
+            write_sys(ds);
+            rebuild_system(s);
+            read_sys(ds);
+        }
+        k = k1;
+    }
+    if (changed) {
+        write_sys(ds);
+        build_plan();
+        prep_positions();
+        CK(cudaStreamSynchronize(stream));
+    }
+    if (n_out) *n_out = n_written;
+    return rc;
+}
+
+// pp_disk::rebuild_vectors (pp_disk.cu:1370-1430) and n_objects::update
+// (red_type.h:568-578) for one system; the slot keeps its capacity.
+void red_sim::rebuild_system(uint32_t s)
+{
+    SysHost& h = sh[s];
+    HostState hs, out;
+    get_host_state(s, hs);
+    const uint32_t n_active = h.n_active();
+    for (uint32_t i = 0; i < h.n; i++) {
+        if (0 < hs.md[i].id && n_active > out.r.size()) {
+            out.r.push_back(hs.r[i]);
+            out.v.push_back(hs.v[i]);
+            out.p.push_back(hs.p[i]);
+            out.md.push_back(hs.md[i]);
+        }
+    }
+    if (out.r.size() != n_active)
+        throw ArgError{RED_ERR_ARG, "Number of copied bodies does not equal to the number of active bodies."};
+    for (int i = 0; i < 7; i++) {
+        h.playing[i] -= h.inactive[i];
+        h.removed[i] += h.inactive[i];
+        h.inactive[i] = 0;
+    }
+    h.n = (uint32_t)out.r.size();
+    if (h.n) put_host_state(s, out);
+    invalidate();
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+#define GUARD_BEGIN try {
+#define GUARD_END                                                                                        \
+    }                                                                                                    \
+    catch (const CudaError& e) {                                                                         \
+        return set_error(RED_ERR_CUDA, "CUDA error %s (%s) at sim.cu:%d: %s", cudaGetErrorName(e.e),   \
+                         cudaGetErrorString(e.e), e.line, e.what);                                     \
+    }                                                                                                    \
+    catch (const ArgError& e) {                                                                          \
+        return set_error(e.code, "%s", e.msg.c_str());                                                   \
+    }                                                                                                    \
+    catch (const std::bad_alloc&) {                                                                      \
+        return set_error(RED_ERR_ARG, "host allocation failed");                                         \
+    }
+
+static int check_sim(red_sim* sim)
+{
+    if (!sim) return set_error(RED_ERR_ARG, "null handle");
+    cudaSetDevice(sim->device);
+    return RED_OK;
+}
+
+extern "C" {
+
+const char* red_last_error(void) { return g_last_error.c_str(); }
+const char* red_version(void) { return "redgb 0.1 (sm_103a)"; }
+
+int red_create(const red_config_t* cfg, uint32_t n_systems, const uint32_t* playing, const red_var4_t* r,
+               const red_var4_t* v, const red_param_t* p, const red_body_metadata_t* md, const double* t0,
+               const double* dt0, red_sim** out)
+{
+    if (!cfg || !playing || !r || !v || !p || !md || !out) return set_error(RED_ERR_ARG, "null argument");
+    *out = nullptr;
+    red_sim* sim = new (std::nothrow) red_sim();
+    if (!sim) return set_error(RED_ERR_ARG, "host allocation failed");
+    try {
+        sim->create(cfg, n_systems, playing, r, v, p, md, t0, dt0);
+    } catch (const CudaError& e) {
+        delete sim;
+        return set_error(RED_ERR_CUDA, "CUDA error %s at sim.cu:%d: %s", cudaGetErrorString(e.e), e.line, e.what);
+    } catch (const ArgError& e) {
+        delete sim;
+        return set_error(e.code, "%s", e.msg.c_str());
+    }
+    *out = sim;
+    return RED_OK;
+}
+
+int red_destroy(red_sim* sim)
+{
+    if (!sim) return RED_OK;
+    cudaSetDevice(sim->device);
+    if (sim->stream) cudaStreamSynchronize(sim->stream);
+    delete sim;
+    return RED_OK;
+}
+
+int red_launch_tries(red_sim* sim, uint32_t n)
+{
+    if (int rc = check_sim(sim)) return rc;
+    GUARD_BEGIN
+    sim->launch_tries(n);
+    return RED_OK;
+    GUARD_END
+}
+
+int red_synchronize(red_sim* sim, uint32_t* n_active, uint32_t* n_halted)
+{
+    if (int rc = check_sim(sim)) return rc;
+    GUARD_BEGIN
+    std::vector<DevSys> ds;
+    sim->read_sys(ds);
+    uint32_t a = 0, h = 0;
+    int status = RED_OK;
+    for (const DevSys& d : ds) {
+        a += d.active ? 1 : 0;
+        h += d.halted ? 1 : 0;
+        if (d.status && !status) status = d.status;
+    }
+    if (n_active) *n_active = a;
+    if (n_halted) *n_halted = h;
+    if (status) return set_error(status, "a system stopped with status %d (non-finite state or error estimate)", status);
+    return RED_OK;
+    GUARD_END
+}
+
+int red_step(red_sim* sim, double* dt_did)
+{
+    if (int rc = check_sim(sim)) return rc;
+    GUARD_BEGIN
+    std::vector<DevSys> ds;
+    sim->read_sys(ds);
+    for (DevSys& d : ds) d.quota = 1;
+    sim->write_sys(ds);
+    // each try is one graph launch; systems stop after one accepted step
+    for (int guard = 0; guard < 100000; guard++) {
+        sim->launch_tries(1);
+        sim->read_sys(ds);
+        bool pending = false;
+        for (const DevSys& d : ds) {
+            if (d.status) {
+                for (DevSys& q : ds) q.quota = -1;
+                sim->write_sys(ds);
+                return set_error(d.status, "integration stopped: status %d", d.status);
+            }
+            if (d.active && !d.halted && d.quota != 0) pending = true;
+        }
+        if (!pending) break;
+    }
+    if (dt_did) *dt_did = ds[0].dt_did;
+    for (DevSys& d : ds) d.quota = -1;
+    sim->write_sys(ds);
+    return RED_OK;
+    GUARD_END
+}
+
+int red_handle_events(red_sim* sim, red_event_t* out, uint32_t cap, uint32_t* n_out)
+{
+    if (int rc = check_sim(sim)) return rc;
+    GUARD_BEGIN
+    return sim->handle_events(out, cap, n_out);
+    GUARD_END
+}
+
+static int check_generic(red_sim* sim, int collision, red_event_t* out, uint32_t cap, uint32_t* n_out)
+{
+    CK(cudaStreamSynchronize(sim->stream));
+    // the explicit check must not see events left by the device-side checks
+    CK(cudaMemsetAsync(sim->d_nev, 0, sizeof(unsigned int), sim->stream));
+    if (collision) {
+        CollParams Q;
+        memset(&Q, 0, sizeof(Q));
+        Q.items = sim->d_pairs; Q.sinfo = sim->d_sinfo; Q.sys = sim->d_sys;
+        Q.pos_hi = sim->pos_hi[0]; Q.pos_lo = sim->pos_lo[0]; Q.y_r = sim->y_r;
+        Q.radius = sim->radius; Q.mass = sim->mass; Q.id = sim->id;
+        Q.factor = sim->cfg.threshold[RED_THRESHOLD_RADII_ENHANCE_FACTOR];
+        Q.only_accepted = 0;
+        Q.mark = 0;
+        Q.events = sim->d_events; Q.n_events = sim->d_nev; Q.capacity = sim->ev_cap;
+        sim->prep_positions();
+        launch_collision(Q, (int)sim->pairs.size(), sim->stream);
+    } else {
+        EjhcParams E;
+        memset(&E, 0, sizeof(E));
+        E.segs = sim->d_segs; E.sinfo = sim->d_sinfo; E.sys = sim->d_sys; E.y_r = sim->y_r;
+        E.id = sim->id; E.btype = sim->btype;
+        E.ejection = sim->cfg.threshold[RED_THRESHOLD_EJECTION_DISTANCE];
+        E.hit_centrum = sim->cfg.threshold[RED_THRESHOLD_HIT_CENTRUM_DISTANCE];
+        E.only_accepted = 0;
+        E.mark = 0;
+        E.events = sim->d_events; E.n_events = sim->d_nev; E.capacity = sim->ev_cap;
+        launch_ejhc(E, (int)sim->segs.size(), sim->stream);
+    }
+    CK(cudaGetLastError());
+    sim->launches++;
+    std::vector<DevEvent> ev;
+    const uint32_t n_raw = sim->collect_events(ev);
+    std::vector<DevSys> ds;
+    sim->read_sys(ds);
+    uint32_t w = 0;
+    uint32_t cur = UINT32_MAX;
+    HostState hs;
+    for (const DevEvent& de : ev) {
+        if ((uint32_t)de.sys != cur) {
+            cur = de.sys;
+            sim->get_host_state(cur, hs);
+        }
+        if (out && w < cap) sim->fill_event(cur, hs, de, ds[cur].t, out[w]);
+        w++;
+    }
+    if (n_out) *n_out = w;
+    if (n_raw > sim->ev_cap)
+        return set_error(RED_ERR_EVENT_OVERFLOW, "%u events exceed the event buffer (%u)", n_raw, sim->ev_cap);
+    return RED_OK;
+}
+
+int red_check_for_collision(red_sim* sim, red_event_t* out, uint32_t cap, uint32_t* n_out)
+{
+    if (int rc = check_sim(sim)) return rc;
+    GUARD_BEGIN
+    return check_generic(sim, 1, out, cap, n_out);
+    GUARD_END
+}
+
+int red_check_for_ejection_hit_centrum(red_sim* sim, red_event_t* out, uint32_t cap, uint32_t* n_out)
+{
+    if (int rc = check_sim(sim)) return rc;
+    GUARD_BEGIN
+    return check_generic(sim, 0, out, cap, n_out);
+    GUARD_END
+}
+
+int red_calc_dydx(red_sim* sim, uint32_t sys, int32_t i, double t, red_var4_t* dy)
+{
+    if (int rc = check_sim(sim)) return rc;
+    if (sys >= sim->n_sys || !dy || (i != 0 && i != 1)) return set_error(RED_ERR_ARG, "bad argument");
+    GUARD_BEGIN
+    const SysHost& h = sim->sh[sys];
+    std::vector<double> buf(3 * (size_t)h.n);
+    CK(cudaStreamSynchronize(sim->stream));
+    if (i == 1) {
+        sim->prep_positions();
+        StageParams P = sim->stage_params(0, true);
+        P.t_standalone = t;
+        // only this system's items
+        std::vector<GravItem> mine;
+        for (const GravItem& g : sim->items)
+            if (g.sys == (int)sys) mine.push_back(g);
+        GravItem* d = dalloc<GravItem>(mine.size());
+        CK(cudaMemcpy(d, mine.data(), mine.size() * sizeof(GravItem), cudaMemcpyHostToDevice));
+        P.items = d;
+        launch_stage(P, (int)mine.size(), sim->mode, sim->cfg.stage_exact, sim->stream);
+        CK(cudaGetLastError());
+        sim->launches++;
+        CK(cudaMemcpyAsync(buf.data(), sim->Kv[0] + 3 * (size_t)h.off, buf.size() * sizeof(double),
+                           cudaMemcpyDeviceToHost, sim->stream));
+        CK(cudaStreamSynchronize(sim->stream));
+        cudaFree(d);
+    } else {
+        CK(cudaMemcpyAsync(buf.data(), sim->y_v + 3 * (size_t)h.off, buf.size() * sizeof(double),
+                           cudaMemcpyDeviceToHost, sim->stream));
+        CK(cudaStreamSynchronize(sim->stream));
+    }
+    for (uint32_t k = 0; k < h.n; k++) dy[k] = red_var4_t{buf[3 * k], buf[3 * k + 1], buf[3 * k + 2], 0.0};
+    return RED_OK;
+    GUARD_END
+}
+
+static int potential(red_sim* sim, uint32_t sys, int interacting, std::vector<double>& u)
+{
+    const SysHost& h = sim->sh[sys];
+    launch_potential(sim->d_segs, (int)sim->segs.size(), sim->d_sinfo, sim->y_r, sim->mass, sim->id, (int)sys,
+                     interacting, sim->d_u, sim->stream);
+    CK(cudaGetLastError());
+    sim->launches++;
+    u.resize(h.n);
+    CK(cudaMemcpyAsync(u.data(), sim->d_u + h.off, h.n * sizeof(double), cudaMemcpyDeviceToHost, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    return RED_OK;
+}
+
+int red_calc_integral(red_sim* sim, uint32_t sys, red_integral_t* out)
+{
+    if (int rc = check_sim(sim)) return rc;
+    if (sys >= sim->n_sys || !out) return set_error(RED_ERR_ARG, "bad argument");
+    GUARD_BEGIN
+    CK(cudaStreamSynchronize(sim->stream));
+    HostState hs;
+    sim->get_host_state(sys, hs);
+    const uint32_t n = (uint32_t)hs.r.size();
+    // tools::get_total_mass, calc_bc, calc_angular_momentum, calc_kinetic_energy (tools.cpp:365-690)
+    double M0 = 0.0, R[3] = {0, 0, 0}, V[3] = {0, 0, 0}, C[3] = {0, 0, 0}, T = 0.0;
+    for (int j = (int)n - 1; j >= 0; j--) {
+        if (0 > hs.md[j].id) continue;
+        M0 += hs.p[j].mass;
+    }
+    for (int j = (int)n - 1; j >= 0; j--) {
+        if (0 > hs.md[j].id) continue;
+        const double m = hs.p[j].mass;
+        R[0] += m * hs.r[j].x; R[1] += m * hs.r[j].y; R[2] += m * hs.r[j].z;
+        V[0] += m * hs.v[j].x; V[1] += m * hs.v[j].y; V[2] += m * hs.v[j].z;
+    }
+    for (uint32_t i = 0; i < n; i++) {
+        if (0 > hs.md[i].id) continue;
+        const red_var4_t& r = hs.r[i];
+        const red_var4_t& v = hs.v[i];
+        const double m = hs.p[i].mass;
+        C[0] += m * (r.y * v.z - r.z * v.y);
+        C[1] += m * (r.z * v.x - r.x * v.z);
+        C[2] += m * (r.x * v.y - r.y * v.x);
+        T += m * (v.x * v.x + v.y * v.y + v.z * v.z);
+    }
+    std::vector<double> u;
+    potential(sim, sys, 0, u);
+    double U = 0.0;
+    for (double x : u) U += x;
+    out->R = red_var4_t{R[0] / M0, R[1] / M0, R[2] / M0, 0.0};
+    out->V = red_var4_t{V[0] / M0, V[1] / M0, V[2] / M0, 0.0};
+    out->C = red_var4_t{C[0], C[1], C[2], 0.0};
+    out->E = T / 2.0 - U / 2.0;
+    return RED_OK;
+    GUARD_END
+}
+
+int red_calc_energy_interacting(red_sim* sim, uint32_t sys, double out[4])
+{
+    if (int rc = check_sim(sim)) return rc;
+    if (sys >= sim->n_sys || !out) return set_error(RED_ERR_ARG, "bad argument");
+    GUARD_BEGIN
+    CK(cudaStreamSynchronize(sim->stream));
+    HostState hs;
+    sim->get_host_state(sys, hs);
+    const uint32_t nm = sim->sh[sys].n_massive();
+    double T = 0.0, C[3] = {0, 0, 0};
+    for (uint32_t i = 0; i < nm && i < hs.r.size(); i++) {
+        if (0 > hs.md[i].id) continue;
+        const red_var4_t& r = hs.r[i];
+        const red_var4_t& v = hs.v[i];
+        const double m = hs.p[i].mass;
+        T += m * (v.x * v.x + v.y * v.y + v.z * v.z);
+        C[0] += m * (r.y * v.z - r.z * v.y);
+        C[1] += m * (r.z * v.x - r.x * v.z);
+        C[2] += m * (r.x * v.y - r.y * v.x);
+    }
+    std::vector<double> u;
+    potential(sim, sys, 1, u);
+    double U = 0.0;
+    for (double x : u) U += x;
+    out[0] = T / 2.0 - U;
+    out[1] = C[0];
+    out[2] = C[1];
+    out[3] = C[2];
+    return RED_OK;
+    GUARD_END
+}
+
+int red_get_state(red_sim* sim, uint32_t sys, red_var4_t* r, red_var4_t* v, red_param_t* p,
+                  red_body_metadata_t* md)
+{
+    if (int rc = check_sim(sim)) return rc;
+    if (sys >= sim->n_sys) return set_error(RED_ERR_ARG, "bad system index");
+    GUARD_BEGIN
+    CK(cudaStreamSynchronize(sim->stream));
+    HostState hs;
+    sim->get_host_state(sys, hs);
+    const size_t n = hs.r.size();
+    if (r) memcpy(r, hs.r.data(), n * sizeof(red_var4_t));
+    if (v) memcpy(v, hs.v.data(), n * sizeof(red_var4_t));
+    if (p) memcpy(p, hs.p.data(), n * sizeof(red_param_t));
+    if (md) memcpy(md, hs.md.data(), n * sizeof(red_body_metadata_t));
+    return RED_OK;
+    GUARD_END
+}
+
+int red_set_state(red_sim* sim, uint32_t sys, const red_var4_t* r, const red_var4_t* v, const red_param_t* p,
+                  const red_body_metadata_t* md)
+{
+    if (int rc = check_sim(sim)) return rc;
+    if (sys >= sim->n_sys) return set_error(RED_ERR_ARG, "bad system index");
+    GUARD_BEGIN
+    CK(cudaStreamSynchronize(sim->stream));
+    HostState hs;
+    sim->get_host_state(sys, hs);
+    const size_t n = hs.r.size();
+    if (r) memcpy(hs.r.data(), r, n * sizeof(red_var4_t));
+    if (v) memcpy(hs.v.data(), v, n * sizeof(red_var4_t));
+    if (p) memcpy(hs.p.data(), p, n * sizeof(red_param_t));
+    if (md) {
+        for (size_t i = 0; i < n; i++)
+            if (md[i].body_type != hs.md[i].body_type)
+                return set_error(RED_ERR_ARG, "body types cannot change through red_set_state");
+        memcpy(hs.md.data(), md, n * sizeof(red_body_metadata_t));
+    }
+    sim->put_host_state(sys, hs);
+    sim->prep_positions();
+    CK(cudaStreamSynchronize(sim->stream));
+    return RED_OK;
+    GUARD_END
+}
+
+int red_get_system_info(red_sim* sim, uint32_t sys, red_system_info_t* info)
+{
+    if (int rc = check_sim(sim)) return rc;
+    if (sys >= sim->n_sys || !info) return set_error(RED_ERR_ARG, "bad argument");
+    GUARD_BEGIN
+    std::vector<DevSys> ds;
+    sim->read_sys(ds);
+    const DevSys& d = ds[sys];
+    const SysHost& h = sim->sh[sys];
+    memset(info, 0, sizeof(*info));
+    info->t = d.t;
+    info->dt_try = d.dt_try;
+    info->dt_did = d.dt_did;
+    info->dt_next = d.dt_next;
+    info->n_tried = d.n_tried;
+    info->n_passed = d.n_passed;
+    info->n_failed = d.n_failed;
+    memcpy(info->playing, h.playing, sizeof(h.playing));
+    memcpy(info->inactive, h.inactive, sizeof(h.inactive));
+    memcpy(info->removed, h.removed, sizeof(h.removed));
+    info->n_total = h.n;
+    info->active = d.active;
+    info->halted = d.halted;
+    info->status = d.status;
+    memcpy(info->n_collision, h.n_collision, sizeof(h.n_collision));
+    memcpy(info->n_ejection, h.n_ejection, sizeof(h.n_ejection));
+    memcpy(info->n_hit_centrum, h.n_hit_centrum, sizeof(h.n_hit_centrum));
+    memcpy(info->n_event, h.n_event, sizeof(h.n_event));
+    return RED_OK;
+    GUARD_END
+}
+
+int red_set_dt_next(red_sim* sim, uint32_t sys, double dt_next)
+{
+    if (int rc = check_sim(sim)) return rc;
+    if (sys >= sim->n_sys) return set_error(RED_ERR_ARG, "bad system index");
+    GUARD_BEGIN
+    std::vector<DevSys> ds;
+    sim->read_sys(ds);
+    ds[sys].dt_next = ds[sys].dt_try = dt_next;
+    sim->write_sys(ds);
+    return RED_OK;
+    GUARD_END
+}
+
+int red_rebuild_vectors(red_sim* sim)
+{
+    if (int rc = check_sim(sim)) return rc;
+    GUARD_BEGIN
+    CK(cudaStreamSynchronize(sim->stream));
+    for (uint32_t s = 0; s < sim->n_sys; s++) sim->rebuild_system(s);
+    sim->build_plan();
+    sim->prep_positions();
+    CK(cudaStreamSynchronize(sim->stream));
+    return RED_OK;
+    GUARD_END
+}
+
+int red_profile_try(red_sim* sim, float* ms, int32_t* kind, uint32_t cap, uint32_t* n_out)
+{
+    if (int rc = check_sim(sim)) return rc;
+    GUARD_BEGIN
+    std::vector<int> kinds;
+    std::vector<cudaEvent_t> evs;
+    sim->enqueue_try(&kinds, &evs);
+    CK(cudaGetLastError());
+    sim->launches += (uint64_t)sim->launches_per_try;
+    CK(cudaStreamSynchronize(sim->stream));
+    uint32_t w = 0;
+    for (size_t k = 1; k < evs.size(); k++) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, evs[k - 1], evs[k]));
+        if (w < cap) {
+            if (ms) ms[w] = t;
+            if (kind) kind[w] = kinds[k];
+        }
+        w++;
+    }
+    for (cudaEvent_t e : evs) cudaEventDestroy(e);
+    if (n_out) *n_out = w;
+    return RED_OK;
+    GUARD_END
+}
+
+uint64_t red_interactions_per_eval(red_sim* sim) { return sim ? sim->interactions_per_eval() : 0; }
+uint64_t red_kernel_launches(red_sim* sim) { return sim ? sim->launches : 0; }
+uint32_t red_n_systems(red_sim* sim) { return sim ? sim->n_sys : 0; }
+
+int red_autotune(red_sim* sim)
+{
+    if (int rc = check_sim(sim)) return rc;
+    GUARD_BEGIN
+    // candidate source chunk sizes; the stage-0 gravity launch is timed on the
+    // current state (standalone, so nothing is integrated)
+    const int cands[] = {0, 128, 256, 512, 1024, 2048, 4096};
+    float best = 1e30f;
+    int best_c = 0;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaStreamSynchronize(sim->stream));
+    sim->prep_positions();
+    for (int c : cands) {
+        if (sim->mode == MODE_FP64_EXACT && c) continue;
+        sim->chunk_override = c;
+        sim->build_plan();
+        StageParams P = sim->stage_params(0, true);
+        for (int w = 0; w < 2; w++) launch_stage(P, (int)sim->items.size(), sim->mode, sim->cfg.stage_exact, sim->stream);
+        CK(cudaEventRecord(e0, sim->stream));
+        const int reps = 5;
+        for (int w = 0; w < reps; w++) launch_stage(P, (int)sim->items.size(), sim->mode, sim->cfg.stage_exact, sim->stream);
+        CK(cudaEventRecord(e1, sim->stream));
+        CK(cudaEventSynchronize(e1));
+        sim->launches += 2 + reps;
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+            best = ms;
+            best_c = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    sim->chunk_override = best_c;
+    sim->build_plan();
+    sim->prep_positions();
+    CK(cudaStreamSynchronize(sim->stream));
+    return RED_OK;
+    GUARD_END
+}
+
+}  // extern "C"

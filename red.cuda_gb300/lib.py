@@ -1,0 +1,282 @@
+"""ctypes binding of libredgb (include/redgb.h) and a Python mirror of the
+pp_disk / integrator seam for tests and benchmarks.
+
+Every call goes through the C ABI; there is no fallback: if libredgb.so
+cannot be loaded, or the device is missing, the calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from .types import BMD, EVENT, PARAM, VAR4, System
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libredgb.so")
+
+RED_OK = 0
+ERRORS = {1: "RED_ERR_ARG", 2: "RED_ERR_CUDA", 3: "RED_ERR_EVENT_OVERFLOW", 4: "RED_ERR_TIMEOUT",
+          5: "RED_ERR_NONFINITE", 6: "RED_ERR_NOT_IMPLEMENTED", 7: "RED_ERR_SUPERPLANETESIMAL",
+          8: "RED_ERR_NO_DEVICE"}
+PRECISION = {"mixed": 0, "fp64": 1, "fp64_exact": 2, "fp32": 3}
+INTEGRATOR = {"rk4": 2, "rkf78": 4, "rkf8": 4}
+
+EXPORTS = ["red_create", "red_destroy", "red_step", "red_launch_tries", "red_synchronize",
+           "red_handle_events", "red_check_for_collision", "red_check_for_ejection_hit_centrum",
+           "red_calc_dydx", "red_calc_integral", "red_calc_energy_interacting", "red_get_state",
+           "red_set_state", "red_get_system_info", "red_set_dt_next", "red_rebuild_vectors",
+           "red_autotune", "red_profile_try", "red_interactions_per_eval", "red_kernel_launches", "red_n_systems",
+           "red_last_error", "red_version"]
+
+
+class RedError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (ERRORS.get(code, code), msg))
+        self.code = code
+
+
+class GasParams(C.Structure):
+    _fields_ = [("rho", C.c_double * 2), ("sch", C.c_double * 2), ("eta", C.c_double * 2),
+                ("tau", C.c_double * 2), ("mfp", C.c_double * 2), ("temp", C.c_double * 2),
+                ("c_vth", C.c_double), ("gas_decrease", C.c_int32), ("t0", C.c_double), ("t1", C.c_double),
+                ("e_folding_time", C.c_double), ("alpha", C.c_double), ("mean_molecular_weight", C.c_double),
+                ("particle_diameter", C.c_double)]
+
+
+class Config(C.Structure):
+    _fields_ = [("integrator", C.c_int32), ("adaptive", C.c_int32), ("tolerance", C.c_double),
+                ("error_check_for_tp", C.c_int32), ("precision", C.c_int32), ("stage_exact", C.c_int32),
+                ("threshold", C.c_double * 3), ("output_interval", C.c_double), ("length", C.c_double),
+                ("gas_disk", C.c_int32), ("gas", GasParams), ("event_capacity", C.c_uint32),
+                ("device", C.c_int32), ("stream", C.c_void_p)]
+
+
+class SystemInfo(C.Structure):
+    _fields_ = [("t", C.c_double), ("dt_try", C.c_double), ("dt_did", C.c_double), ("dt_next", C.c_double),
+                ("n_tried", C.c_uint64), ("n_passed", C.c_uint64), ("n_failed", C.c_uint64),
+                ("playing", C.c_uint32 * 7), ("inactive", C.c_uint32 * 7), ("removed", C.c_uint32 * 7),
+                ("n_total", C.c_uint32), ("active", C.c_int32), ("halted", C.c_int32), ("status", C.c_int32),
+                ("n_collision", C.c_uint32 * 3), ("n_ejection", C.c_uint32 * 3),
+                ("n_hit_centrum", C.c_uint32 * 3), ("n_event", C.c_uint32 * 3)]
+
+
+class Integral(C.Structure):
+    _fields_ = [("R", C.c_double * 4), ("V", C.c_double * 4), ("C", C.c_double * 4), ("E", C.c_double)]
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Loads libredgb.so (built by build.py); raises if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("libredgb.so not built (%s); run __graft_entry__.build()" % path)
+    L = C.CDLL(path)
+    P = C.c_void_p
+    u32p = C.POINTER(C.c_uint32)
+    L.red_create.argtypes = [C.POINTER(Config), C.c_uint32, u32p, P, P, P, P, P, P, C.POINTER(C.c_void_p)]
+    L.red_destroy.argtypes = [P]
+    L.red_step.argtypes = [P, C.POINTER(C.c_double)]
+    L.red_launch_tries.argtypes = [P, C.c_uint32]
+    L.red_synchronize.argtypes = [P, u32p, u32p]
+    L.red_handle_events.argtypes = [P, P, C.c_uint32, u32p]
+    L.red_check_for_collision.argtypes = [P, P, C.c_uint32, u32p]
+    L.red_check_for_ejection_hit_centrum.argtypes = [P, P, C.c_uint32, u32p]
+    L.red_calc_dydx.argtypes = [P, C.c_uint32, C.c_int32, C.c_double, P]
+    L.red_calc_integral.argtypes = [P, C.c_uint32, C.POINTER(Integral)]
+    L.red_calc_energy_interacting.argtypes = [P, C.c_uint32, P]
+    L.red_get_state.argtypes = [P, C.c_uint32, P, P, P, P]
+    L.red_set_state.argtypes = [P, C.c_uint32, P, P, P, P]
+    L.red_get_system_info.argtypes = [P, C.c_uint32, C.POINTER(SystemInfo)]
+    L.red_set_dt_next.argtypes = [P, C.c_uint32, C.c_double]
+    L.red_rebuild_vectors.argtypes = [P]
+    L.red_autotune.argtypes = [P]
+    L.red_profile_try.argtypes = [P, P, P, C.c_uint32, u32p]
+    L.red_interactions_per_eval.argtypes = [P]
+    L.red_interactions_per_eval.restype = C.c_uint64
+    L.red_kernel_launches.argtypes = [P]
+    L.red_kernel_launches.restype = C.c_uint64
+    L.red_n_systems.argtypes = [P]
+    L.red_n_systems.restype = C.c_uint32
+    L.red_last_error.restype = C.c_char_p
+    L.red_version.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _check(rc):
+    if rc != RED_OK:
+        raise RedError(rc, load().red_last_error().decode())
+
+
+def gas_struct(gas_record):
+    """numpy GAS record (types.GAS) -> GasParams."""
+    g = GasParams()
+    C.memmove(C.addressof(g), np.ascontiguousarray(gas_record).tobytes(), C.sizeof(GasParams))
+    return g
+
+
+class Sim:
+    """One handle of libredgb holding one or more systems."""
+
+    def __init__(self, systems, *, integrator="rkf78", adaptive=True, tolerance=1e-10, dt=None,
+                 precision="mixed", stage_exact=False, collision_factor=0.0, ejection=0.0,
+                 hit_centrum=0.0, gas=None, output_interval=0.0, length=0.0, error_check_for_tp=False,
+                 event_capacity=0, device=0, stream=None, t0=None):
+        L = load()
+        if isinstance(systems, System):
+            systems = [systems]
+        self.systems_n = [s.n for s in systems]
+        cfg = Config()
+        cfg.integrator = INTEGRATOR[integrator] if isinstance(integrator, str) else int(integrator)
+        cfg.adaptive = int(adaptive)
+        cfg.tolerance = tolerance
+        cfg.error_check_for_tp = int(error_check_for_tp)
+        cfg.precision = PRECISION[precision] if isinstance(precision, str) else int(precision)
+        cfg.stage_exact = int(stage_exact)
+        cfg.threshold[0] = hit_centrum
+        cfg.threshold[1] = ejection
+        cfg.threshold[2] = collision_factor
+        cfg.output_interval = output_interval
+        cfg.length = length
+        if gas is not None:
+            cfg.gas_disk = 1
+            cfg.gas = gas_struct(gas)
+        cfg.event_capacity = event_capacity
+        cfg.device = device
+        cfg.stream = stream
+        self.cfg = cfg
+        playing = np.concatenate([s.playing for s in systems]).astype(np.uint32)
+        # np.concatenate packs structured dtypes (a 20-byte metadata record); keep red's layout
+        r = np.concatenate([s.r for s in systems]).astype(VAR4)
+        v = np.concatenate([s.v for s in systems]).astype(VAR4)
+        p = np.concatenate([s.p for s in systems]).astype(PARAM)
+        md = np.concatenate([s.md for s in systems]).astype(BMD)
+        assert md.itemsize == 24
+        ns = len(systems)
+        dts = np.broadcast_to(np.asarray(dt if dt is not None else 0.0, dtype=np.float64), (ns,)).copy()
+        t0s = np.broadcast_to(np.asarray(t0 if t0 is not None else 0.0, dtype=np.float64), (ns,)).copy()
+        h = C.c_void_p()
+        _check(L.red_create(C.byref(cfg), ns, playing.ctypes.data_as(C.POINTER(C.c_uint32)), _p(r), _p(v),
+                            _p(p), _p(md), _p(t0s), _p(dts), C.byref(h)))
+        self.h = h
+        self.n_systems = ns
+        self.names = [s.names for s in systems]
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().red_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- integrator::step and the device-side loop --------------------------
+    def step(self):
+        d = C.c_double()
+        _check(load().red_step(self.h, C.byref(d)))
+        return d.value
+
+    def launch_tries(self, n):
+        _check(load().red_launch_tries(self.h, n))
+
+    def synchronize(self):
+        a, h = C.c_uint32(), C.c_uint32()
+        _check(load().red_synchronize(self.h, C.byref(a), C.byref(h)))
+        return a.value, h.value
+
+    def handle_events(self, cap=4096):
+        out = np.zeros(cap, EVENT)
+        n = C.c_uint32()
+        _check(load().red_handle_events(self.h, _p(out), cap, C.byref(n)))
+        return out[:min(n.value, cap)].copy()
+
+    def check_for_collision(self, cap=4096):
+        out = np.zeros(cap, EVENT)
+        n = C.c_uint32()
+        _check(load().red_check_for_collision(self.h, _p(out), cap, C.byref(n)))
+        return out[:min(n.value, cap)].copy()
+
+    def check_for_ejection_hit_centrum(self, cap=4096):
+        out = np.zeros(cap, EVENT)
+        n = C.c_uint32()
+        _check(load().red_check_for_ejection_hit_centrum(self.h, _p(out), cap, C.byref(n)))
+        return out[:min(n.value, cap)].copy()
+
+    # -- pp_disk seam ---------------------------------------------------------
+    def info(self, sys=0):
+        i = SystemInfo()
+        _check(load().red_get_system_info(self.h, sys, C.byref(i)))
+        return i
+
+    def calc_dydx(self, sys, i, t):
+        n = self.info(sys).n_total
+        dy = np.zeros(n, VAR4)
+        _check(load().red_calc_dydx(self.h, sys, i, t, _p(dy)))
+        return dy
+
+    def calc_integral(self, sys=0):
+        I = Integral()
+        _check(load().red_calc_integral(self.h, sys, C.byref(I)))
+        return np.array(list(I.R)[:3] + list(I.V)[:3] + list(I.C)[:3] + [I.E])
+
+    def energy_interacting(self, sys=0):
+        out = np.zeros(4)
+        _check(load().red_calc_energy_interacting(self.h, sys, _p(out)))
+        return out
+
+    def get_state(self, sys=0):
+        info = self.info(sys)
+        n = info.n_total
+        r, v, p, md = np.zeros(n, VAR4), np.zeros(n, VAR4), np.zeros(n, PARAM), np.zeros(n, BMD)
+        _check(load().red_get_state(self.h, sys, _p(r), _p(v), _p(p), _p(md)))
+        s = System(r, v, p, md, np.array(info.playing, np.uint32))
+        s.inactive = np.array(info.inactive, np.uint32)
+        s.removed = np.array(info.removed, np.uint32)
+        return s
+
+    def set_state(self, sys, s):
+        _check(load().red_set_state(self.h, sys, _p(np.ascontiguousarray(s.r, VAR4)),
+                                    _p(np.ascontiguousarray(s.v, VAR4)), _p(np.ascontiguousarray(s.p, PARAM)),
+                                    _p(np.ascontiguousarray(s.md, BMD))))
+
+    def set_dt_next(self, sys, dt):
+        _check(load().red_set_dt_next(self.h, sys, dt))
+
+    def rebuild_vectors(self):
+        _check(load().red_rebuild_vectors(self.h))
+
+    def autotune(self):
+        _check(load().red_autotune(self.h))
+
+    def profile_try(self, cap=64):
+        """Durations (ms) and kinds of the launches of one try, run kernel by kernel."""
+        ms = np.zeros(cap, np.float32)
+        kind = np.zeros(cap, np.int32)
+        n = C.c_uint32()
+        _check(load().red_profile_try(self.h, _p(ms), _p(kind), cap, C.byref(n)))
+        return ms[:n.value].copy(), kind[:n.value].copy()
+
+    @property
+    def interactions_per_eval(self):
+        return int(load().red_interactions_per_eval(self.h))
+
+    @property
+    def kernel_launches(self):
+        return int(load().red_kernel_launches(self.h))
