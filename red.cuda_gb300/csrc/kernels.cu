@@ -47,6 +47,16 @@ __device__ __forceinline__ void ds_add(float& hi, float& lo, float t)
     lo += e;
 }
 
+// (ah, al) += (bh, bl) for double-single values (TwoSum on the high words,
+// low words added; Dekker 1971 / Knuth TwoSum).
+__device__ __forceinline__ void ds_merge(float& ah, float& al, float bh, float bl)
+{
+    float s, e;
+    two_sum(ah, bh, s, e);
+    ah = s;
+    al = al + bl + e;
+}
+
 __device__ __forceinline__ void split_ds(double x, float& h, float& l)
 {
     h = __double2float_rn(x);
@@ -102,14 +112,17 @@ __device__ double gas_reduction_factor(const GasDev& g, double t)
     }
 }
 
-__device__ void drag_accel(const GasDev& g, double decr, double m_star, double rx, double ry, double rz,
-                           double vx, double vy, double vz, double cd, double radius, double density,
-                           double& ax, double& ay, double& az)
+// Drag factor f and gas velocity (gx, gy, 0) at (r, v): the acceleration is
+// f (v_gas - v) (calc_drag_accel_NSI, pp_disk.cu:485-521).
+__device__ void drag_factor(const GasDev& g, double decr, double m_star, double rx, double ry, double rz, double vx,
+                            double vy, double vz, double cd, double radius, double density, double& f, double& gx,
+                            double& gy)
 {
     // gas velocity: circular velocity scaled by sqrt(1 - 2 eta r^p) (pp_disk.cu:107-155)
     const double r = sqrt(rx * rx + ry * ry);
     const double vc = sqrt(m_star / r);
-    double gx = 0.0, gy = 0.0;
+    gx = 0.0;
+    gy = 0.0;
     if (rx == 0.0 && ry == 0.0) {
     } else if (ry == 0.0) {
         gy = rx > 0.0 ? vc : -vc;
@@ -139,79 +152,72 @@ __device__ void drag_accel(const GasDev& g, double decr, double m_star, double r
     }
     const double ux = gx - vx, uy = gy - vy, uz = 0.0 - vz;
     const double un = sqrt(ux * ux + uy * uy + uz * uz);
-    const double f = decr * (3.0 * cd * dens * un) / (8.0 * radius * density);
-    ax += f * ux;
-    ay += f * uy;
-    az += f * uz;
+    f = decr * (3.0 * cd * dens * un) / (8.0 * radius * density);
 }
 
-// ---------------------------------------------------------------------------
-// stage kernel
-// ---------------------------------------------------------------------------
 struct alignas(32) D4 {
     double x, y, z, w;
 };
 
-struct SmemStage {
-    union {
-        struct { float4 hi[kTile]; float4 lo[kTile]; } f;
-        struct { D4 d[kTile]; int id[kTile]; } d;
-    } src;
-    double red[kTile][3];
-    unsigned long long emax[kTile / 32];
-    int last;
-};
+// Nonzero terms of each RKF7(8) stage row in the order red's stage kernels
+// add them (rk8_kernel::calc_ytemp_for_f1..f12, int_rungekutta8.cu:80-246).
+// Compile-time copies of Tableau::nnz / src so that the combination unrolls.
+__device__ constexpr int kNnz[13] = {0, 1, 2, 2, 3, 3, 4, 4, 6, 7, 8, 6, 9};
+__device__ constexpr int kSrc[13][9] = {
+    {0}, {0}, {0, 1}, {0, 2}, {0, 2, 3}, {0, 3, 4}, {0, 3, 4, 5}, {0, 4, 5, 6},
+    {0, 3, 4, 5, 6, 7}, {0, 3, 4, 5, 6, 7, 8}, {0, 3, 4, 5, 6, 7, 8, 9},
+    {0, 5, 6, 7, 8, 9}, {0, 3, 4, 5, 6, 7, 8, 9, 11}};
 
-template <int MODE>
-__device__ __forceinline__ void load_sources(SmemStage& sm, const StageParams& P, int j0, int nj)
+// Component x (= 3 i + c) of the ytemp of RKF7(8) stage NX:
+// y + dt * sum_q a_{NX,q} K_q, terms in red's order; loads issued first.
+template <int NX, bool EXACT>
+__device__ __forceinline__ void combine_rkf78(const StageParams& P, double dt, int x, double& out_r, double& out_v)
 {
-    const int t = threadIdx.x;
-    if (t < nj) {
-        const int j = j0 + t;
-        if (MODE == MODE_MIXED || MODE == MODE_FP32) {
-            sm.src.f.hi[t] = P.pos_hi_in[j];
-            if (MODE == MODE_MIXED) sm.src.f.lo[t] = P.pos_lo_in[j];
-        } else {
-            const int idj = P.id[j];
-            const double m = P.mass[j];
-            sm.src.d.d[t] = D4{P.r_in[3 * j], P.r_in[3 * j + 1], P.r_in[3 * j + 2],
-                                (MODE == MODE_FP64 && idj < 0) ? 0.0 : m};
-            sm.src.d.id[t] = idj;
-        }
+    constexpr int nnz = kNnz[NX];
+    constexpr int off = 1 + NX * (NX - 1) / 2;
+    double kr[nnz], kv[nnz];
+#pragma unroll
+    for (int q = 0; q < nnz; q++) {
+        kr[q] = P.Kr[kSrc[NX][q]][x];
+        kv[q] = P.Kv[kSrc[NX][q]][x];
     }
+    double ar = mul<EXACT>(c_tb.a[off + kSrc[NX][0]], kr[0]);
+    double av = mul<EXACT>(c_tb.a[off + kSrc[NX][0]], kv[0]);
+#pragma unroll
+    for (int q = 1; q < nnz; q++) {
+        const double aq = c_tb.a[off + kSrc[NX][q]];
+        ar = madd<EXACT>(ar, aq, kr[q]);
+        av = madd<EXACT>(av, aq, kv[q]);
+    }
+    out_r = madd<EXACT>(P.y_r[x], dt, ar);
+    out_v = madd<EXACT>(P.y_v[x], dt, av);
 }
 
-// Stage combination for body i: ytemp of stage `nx` (RKF78: y + dt*sum a K,
-// red's term order; RK4: y + (a dt) K).
+// Component x of the ytemp of stage nx (RKF78: y + dt*sum a K in red's term
+// order; RK4: y + (a dt) K, rk4_kernel::sum_vector, int_rungekutta4.cu:36-47).
 template <bool EXACT>
-__device__ __forceinline__ void combine(const StageParams& P, int scheme, int nx, double dt, int i,
-                                        double out_r[3], double out_v[3])
+__device__ __forceinline__ void combine(const StageParams& P, int scheme, int nx, double dt, int x, double& out_r,
+                                        double& out_v)
 {
     if (scheme == SCHEME_RKF78) {
-        const int nnz = c_tb.nnz[nx];
-        const int off = 1 + nx * (nx - 1) / 2;
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            int q0 = c_tb.src[nx][0];
-            double ar = mul<EXACT>(c_tb.a[off + q0], P.Kr[q0][3 * i + c]);
-            double av = mul<EXACT>(c_tb.a[off + q0], P.Kv[q0][3 * i + c]);
-            for (int q = 1; q < nnz; q++) {
-                const int sq = c_tb.src[nx][q];
-                const double aq = c_tb.a[off + sq];
-                ar = madd<EXACT>(ar, aq, P.Kr[sq][3 * i + c]);
-                av = madd<EXACT>(av, aq, P.Kv[sq][3 * i + c]);
-            }
-            out_r[c] = madd<EXACT>(P.y_r[3 * i + c], dt, ar);
-            out_v[c] = madd<EXACT>(P.y_v[3 * i + c], dt, av);
+        switch (nx) {
+        case 1: combine_rkf78<1, EXACT>(P, dt, x, out_r, out_v); break;
+        case 2: combine_rkf78<2, EXACT>(P, dt, x, out_r, out_v); break;
+        case 3: combine_rkf78<3, EXACT>(P, dt, x, out_r, out_v); break;
+        case 4: combine_rkf78<4, EXACT>(P, dt, x, out_r, out_v); break;
+        case 5: combine_rkf78<5, EXACT>(P, dt, x, out_r, out_v); break;
+        case 6: combine_rkf78<6, EXACT>(P, dt, x, out_r, out_v); break;
+        case 7: combine_rkf78<7, EXACT>(P, dt, x, out_r, out_v); break;
+        case 8: combine_rkf78<8, EXACT>(P, dt, x, out_r, out_v); break;
+        case 9: combine_rkf78<9, EXACT>(P, dt, x, out_r, out_v); break;
+        case 10: combine_rkf78<10, EXACT>(P, dt, x, out_r, out_v); break;
+        case 11: combine_rkf78<11, EXACT>(P, dt, x, out_r, out_v); break;
+        default: combine_rkf78<12, EXACT>(P, dt, x, out_r, out_v); break;
         }
     } else {
-        // rk4_kernel::sum_vector: y + (a[r] * dt) * f_{r-1} (int_rungekutta4.cu:36-47, 111-129)
         const double bf = mul<EXACT>(c_tb.a4[nx], dt);
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            out_r[c] = madd<EXACT>(P.y_r[3 * i + c], bf, P.Kr[nx - 1][3 * i + c]);
-            out_v[c] = madd<EXACT>(P.y_v[3 * i + c], bf, P.Kv[nx - 1][3 * i + c]);
-        }
+        out_r = madd<EXACT>(P.y_r[x], bf, P.Kr[nx - 1][x]);
+        out_v = madd<EXACT>(P.y_v[x], bf, P.Kv[nx - 1][x]);
     }
 }
 
@@ -237,90 +243,67 @@ __device__ __forceinline__ double rk8_ynp1(double y, double dt, const double* co
     return madd<EXACT>(y, dt, acc);
 }
 
-template <int MODE, bool EXACT>
-__device__ __forceinline__ double stage_epilogue(const StageParams& P, const GravItem& it, DevSys* S, int i,
-                                                 double ax, double ay, double az)
+// Writes one component of a stage position: the hi / lo words of coordinate c
+// (c < 3), or the mass of the source and the radius (c == 3).
+__device__ __forceinline__ void write_pos_c(float4* hi, float4* lo, int i, int c, double v)
 {
-    const SysInfo si = P.sinfo[it.sys];
-    const int s = P.stage;
-    const double rx = P.r_in[3 * i], ry = P.r_in[3 * i + 1], rz = P.r_in[3 * i + 2];
-    const int idi = P.id[i];
-    if (idi > 0) {
-        if (MODE == MODE_MIXED || MODE == MODE_FP32) {
-            // central-star term in FP64 with red's pair formula (pp_disk.cu:399-413)
-            double sx = 0.0, sy = 0.0, sz = 0.0;
-            for (int j = si.off; j < si.off + si.n_star; j++) {
-                if (j == i || P.id[j] < 0) continue;
-                const double dx = P.r_in[3 * j] - rx, dy = P.r_in[3 * j + 1] - ry, dz = P.r_in[3 * j + 2] - rz;
-                const double w = dx * dx + dy * dy + dz * dz;
-                const double d = sqrt(w);
-                const double f = P.mass[j] / (d * w);
-                sx += f * dx;
-                sy += f * dy;
-                sz += f * dz;
-            }
-            ax = sx + ax;
-            ay = sy + ay;
-            az = sz + az;
-        }
-    } else {
-        ax = ay = az = 0.0;   // calc_grav_accel_naive zeroes inactive sinks (pp_disk.cu:386-388)
+    float* H = reinterpret_cast<float*>(hi + i);
+    float* L = reinterpret_cast<float*>(lo + i);
+    if (c < 3) {
+        float h, l;
+        split_ds(v, h, l);
+        H[c] = h;
+        L[c] = l;
     }
-    const double dt = S->dt_try;
-    if (P.gas.enabled && it.cls == CLS_NSI) {
-        const double ts = P.standalone ? P.t_standalone
-                                       : S->t + (P.scheme == SCHEME_RKF78 ? c_tb.c[s] : c_tb.c4[s]) * dt;
-        const double decr = gas_reduction_factor(P.gas, ts);
-        if (!(1.0e-6 > decr)) {
-            drag_accel(P.gas, decr, P.mass[si.off], rx, ry, rz, P.Kr[s][3 * i], P.Kr[s][3 * i + 1],
-                       P.Kr[s][3 * i + 2], P.cd[i], P.radius[i], P.density[i], ax, ay, az);
-        }
-    }
-    P.Kv[s][3 * i] = ax;
-    P.Kv[s][3 * i + 1] = ay;
-    P.Kv[s][3 * i + 2] = az;
-    if (P.standalone) return 0.0;
+}
 
-    if (P.next >= 0) {
-        double orr[3], ovv[3];
-        if (P.ynp1_to_out) {
-            const double b0 = mul<EXACT>(c_tb.b4[0], dt), b1 = mul<EXACT>(c_tb.b4[1], dt);
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                const int x = 3 * i + c;
-                orr[c] = rk4_ynp1<EXACT>(P.y_r[x], b0, b1, P.Kr[0][x], P.Kr[1][x], P.Kr[2][x], P.Kr[3][x]);
-                ovv[c] = rk4_ynp1<EXACT>(P.y_v[x], b0, b1, P.Kv[0][x], P.Kv[1][x], P.Kv[2][x], P.Kv[3][x]);
-            }
+// ---------------------------------------------------------------------------
+// stage kernel
+//
+// Thread layout: each sink is served by `lanes` consecutive threads of one
+// warp (lanes in {4, 8, 16, 32}).  The lanes split the sources of every
+// shared-memory tile; their partial sums are combined with a butterfly of
+// shuffles (IEEE addition is commutative, so every lane ends with the same
+// bits).  In the epilogue lanes 0, 1, 2 own the x, y, z components and lane 3
+// computes the scalar parts (star term factor, drag factor) and broadcasts them.
+// ---------------------------------------------------------------------------
+constexpr int kStarBatch = 4;   // star factors formed per pass of the epilogue
+
+struct SmemStage {
+    union {
+        struct { float4 hi[kTile]; float4 lo[kTile]; } f;
+        struct { D4 d[kTile]; int id[kTile]; } d;
+    } src;
+    double acc[3 * kTile];          // per (sink, component) gravity sums
+    double sc[kTile][3];            // drag factor and gas velocity per sink
+    double fs[kTile][kStarBatch];   // star factors per sink
+    int last;
+};
+
+template <int MODE>
+__device__ __forceinline__ void load_sources(SmemStage& sm, const StageParams& P, int j0, int nj)
+{
+    const int t = threadIdx.x;
+    if (t < nj) {
+        const int j = j0 + t;
+        if (MODE == MODE_MIXED || MODE == MODE_FP32) {
+            sm.src.f.hi[t] = P.pos_hi_in[j];
+            if (MODE == MODE_MIXED) sm.src.f.lo[t] = P.pos_lo_in[j];
         } else {
-            combine<EXACT>(P, P.scheme, P.next, dt, i, orr, ovv);
-        }
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            P.r_out[3 * i + c] = orr[c];
-            P.Kr[P.next][3 * i + c] = ovv[c];
-        }
-        write_pos(P.pos_hi_out, P.pos_lo_out, i, orr[0], orr[1], orr[2], idi >= 0 ? P.mass[i] : 0.0, P.radius[i]);
-    }
-    double e = 0.0;
-    if (P.err_after && i - si.off < si.n_err) {
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            const int x = 3 * i + c;
-            double er, ev;
-            if (P.scheme == SCHEME_RKF78) {
-                // rk8_kernel::calc_error, int_rungekutta8.cu:248-260
-                er = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(P.Kr[0][x], P.Kr[10][x]), P.Kr[11][x]), P.Kr[12][x]));
-                ev = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(P.Kv[0][x], P.Kv[10][x]), P.Kv[11][x]), P.Kv[12][x]));
-            } else {
-                // rk4_kernel::calc_error, int_rungekutta4.cu:62-73
-                er = fabs(P.Kr[3][x] - P.Kr[4][x]);
-                ev = fabs(P.Kv[3][x] - P.Kv[4][x]);
-            }
-            e = fmax(e, fmax(er, ev));
-            if (er != er || ev != ev) e = __longlong_as_double(0x7ff8000000000000ll);
+            const int idj = P.id[j];
+            const double m = P.mass[j];
+            sm.src.d.d[t] = D4{P.r_in[3 * j], P.r_in[3 * j + 1], P.r_in[3 * j + 2],
+                                (MODE == MODE_FP64 && idj < 0) ? 0.0 : m};
+            sm.src.d.id[t] = idj;
         }
     }
-    return e;
+}
+
+// Sum over the `lanes` threads of a sink (aligned groups inside a warp).
+__device__ __forceinline__ double group_sum(double v, int lanes)
+{
+    for (int o = 1; o < lanes; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
 }
 
 template <int MODE, bool EXACT>
@@ -331,23 +314,19 @@ __global__ void __launch_bounds__(kTile) k_stage(const StageParams P)
     DevSys* S = P.sys + it.sys;
     if (!P.standalone && !runnable(*S)) return;   // uniform over the CTA
 
-    // lanes threads per sink: thread t works on sink t % nsink over the sources
-    // j = sub_lane, sub_lane + lanes, ... of every tile
     const int L = it.lanes;
-    const int SP = it.nsink;
-    const int k = threadIdx.x % SP;
-    const int sub_lane = threadIdx.x / SP;
-    const bool has = sub_lane < L;
-    const int i = it.sink0 + k;
+    const int k = threadIdx.x / L;                // sink slot
+    const int lane = threadIdx.x % L;
+    const bool has = k < it.nsink;
+    const int i = it.sink0 + (has ? k : 0);       // inactive slots shadow sink 0 (results unused)
+    const int gbase = (threadIdx.x & 31) & ~(L - 1);   // first lane of the group in the warp
 
     double ax = 0.0, ay = 0.0, az = 0.0;
 
     if (MODE == MODE_MIXED || MODE == MODE_FP32) {
-        float4 H = make_float4(0.f, 0.f, 0.f, 0.f), Lo = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (has) {
-            H = P.pos_hi_in[i];
-            if (MODE == MODE_MIXED) Lo = P.pos_lo_in[i];
-        }
+        const float4 H = P.pos_hi_in[i];
+        float4 Lo = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (MODE == MODE_MIXED) Lo = P.pos_lo_in[i];
         float sxh = 0.f, sxl = 0.f, syh = 0.f, syl = 0.f, szh = 0.f, szl = 0.f;
         for (int j0 = it.src0; j0 < it.src1; j0 += kTile) {
             const int nj = min(kTile, it.src1 - j0);
@@ -357,7 +336,7 @@ __global__ void __launch_bounds__(kTile) k_stage(const StageParams P)
             if (has) {
                 float tx = 0.f, ty = 0.f, tz = 0.f;
 #pragma unroll 4
-                for (int jj = sub_lane; jj < nj; jj += L) {
+                for (int jj = lane; jj < nj; jj += L) {
                     const float4 h = sm.src.f.hi[jj];
                     float dx, dy, dz;
                     if (MODE == MODE_MIXED) {
@@ -383,73 +362,87 @@ __global__ void __launch_bounds__(kTile) k_stage(const StageParams P)
                 ds_add(szh, szl, tz);
             }
         }
-        ax = (double)sxh + (double)sxl;
-        ay = (double)syh + (double)syl;
-        az = (double)szh + (double)szl;
-    } else {
-        double xi = 0.0, yi = 0.0, zi = 0.0;
-        if (has) {
-            xi = P.r_in[3 * i];
-            yi = P.r_in[3 * i + 1];
-            zi = P.r_in[3 * i + 2];
+        // lanes -> one double-single sum (TwoSum in FP32, a fixed butterfly), then lane c
+        // converts component c to FP64 (FP64 work is scarce on this part)
+        for (int o = 1; o < L; o <<= 1) {
+            ds_merge(sxh, sxl, __shfl_xor_sync(0xffffffffu, sxh, o), __shfl_xor_sync(0xffffffffu, sxl, o));
+            ds_merge(syh, syl, __shfl_xor_sync(0xffffffffu, syh, o), __shfl_xor_sync(0xffffffffu, syl, o));
+            ds_merge(szh, szl, __shfl_xor_sync(0xffffffffu, szh, o), __shfl_xor_sync(0xffffffffu, szl, o));
         }
+        const int cl = lane < 3 ? lane : 0;
+        const float hh = cl == 0 ? sxh : (cl == 1 ? syh : szh);
+        const float ll = cl == 0 ? sxl : (cl == 1 ? syl : szl);
+        const double v = lane < 3 ? (double)hh + (double)ll : 0.0;
+        ax = ay = az = v;   // lane c holds component c in all three
+    } else {
+        const double xi = P.r_in[3 * i], yi = P.r_in[3 * i + 1], zi = P.r_in[3 * i + 2];
         for (int j0 = it.src0; j0 < it.src1; j0 += kTile) {
             const int nj = min(kTile, it.src1 - j0);
             __syncthreads();
             load_sources<MODE>(sm, P, j0, nj);
             __syncthreads();
-            if (has) {
-                for (int jj = sub_lane; jj < nj; jj += L) {
+            if (!has) continue;
+            if (MODE == MODE_FP64_EXACT) {
+                // calc_grav_accel_naive, pp_disk.cu:389-413, bit for bit: lane 0 alone,
+                // sources in index order
+                if (lane != 0) continue;
+                for (int jj = 0; jj < nj; jj++) {
                     const D4 q = sm.src.d.d[jj];
-                    if (MODE == MODE_FP64_EXACT) {
-                        // calc_grav_accel_naive, pp_disk.cu:389-413, bit for bit
-                        if (j0 + jj == i || 0 > sm.src.d.id[jj]) continue;
-                        const double dx = __dsub_rn(q.x, xi), dy = __dsub_rn(q.y, yi), dz = __dsub_rn(q.z, zi);
-                        double w = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-                        const double d = __dsqrt_rn(w);
-                        w = __ddiv_rn(q.w, __dmul_rn(d, w));
-                        ax = __dadd_rn(ax, __dmul_rn(w, dx));
-                        ay = __dadd_rn(ay, __dmul_rn(w, dy));
-                        az = __dadd_rn(az, __dmul_rn(w, dz));
-                    } else {
-                        const double dx = q.x - xi, dy = q.y - yi, dz = q.z - zi;
-                        const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
-                        double ri = rsqrt(r2);
-                        ri = r2 > 0.0 ? ri : 0.0;
-                        const double sc = q.w * ri * ri * ri;
-                        ax = fma(sc, dx, ax);
-                        ay = fma(sc, dy, ay);
-                        az = fma(sc, dz, az);
-                    }
+                    if (j0 + jj == i || 0 > sm.src.d.id[jj]) continue;
+                    const double dx = __dsub_rn(q.x, xi), dy = __dsub_rn(q.y, yi), dz = __dsub_rn(q.z, zi);
+                    double w = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+                    const double d = __dsqrt_rn(w);
+                    w = __ddiv_rn(q.w, __dmul_rn(d, w));
+                    ax = __dadd_rn(ax, __dmul_rn(w, dx));
+                    ay = __dadd_rn(ay, __dmul_rn(w, dy));
+                    az = __dadd_rn(az, __dmul_rn(w, dz));
+                }
+            } else {
+                for (int jj = lane; jj < nj; jj += L) {
+                    const D4 q = sm.src.d.d[jj];
+                    const double dx = q.x - xi, dy = q.y - yi, dz = q.z - zi;
+                    const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+                    double ri = rsqrt(r2);
+                    ri = r2 > 0.0 ? ri : 0.0;
+                    const double sc = q.w * ri * ri * ri;
+                    ax = fma(sc, dx, ax);
+                    ay = fma(sc, dy, ay);
+                    az = fma(sc, dz, az);
                 }
             }
         }
     }
 
-    // lanes of one sink -> one sum, fixed order
-    if (L > 1) {
-        __syncthreads();
-        sm.red[threadIdx.x][0] = ax;
-        sm.red[threadIdx.x][1] = ay;
-        sm.red[threadIdx.x][2] = az;
-        __syncthreads();
-        if (sub_lane == 0) {
-            for (int q = 1; q < L; q++) {
-                ax += sm.red[k + q * SP][0];
-                ay += sm.red[k + q * SP][1];
-                az += sm.red[k + q * SP][2];
-            }
-        }
+    // FP64 modes: lanes of one sink -> one sum, the same bits on every lane
+    if (MODE == MODE_FP64_EXACT) {
+        ax = __shfl_sync(0xffffffffu, ax, gbase);
+        ay = __shfl_sync(0xffffffffu, ay, gbase);
+        az = __shfl_sync(0xffffffffu, az, gbase);
+    } else if (MODE == MODE_FP64) {
+        ax = group_sum(ax, L);
+        ay = group_sum(ay, L);
+        az = group_sum(az, L);
     }
-    const bool owner = (sub_lane == 0) && has;
+    // lane c of each sink holds component c (FP32 modes: ax = ay = az = component c)
+    const double mine = lane == 0 ? ax : (lane == 1 ? ay : az);
 
-    // source chunks of one sink tile -> the CTA that finishes last reduces them
+    // ---- from here on the CTA works element-wise: thread t < 3 nsink owns
+    // component x = 3 sink0 + t (contiguous in HBM), so every FP64 instruction
+    // runs in full warps; scalars per sink are formed by thread t < nsink ----
+    const int nel = 3 * it.nsink;
+    const int t = threadIdx.x;
+    const bool elem = t < nel;
+    const int ke = elem ? t / 3 : 0;          // sink slot of the element
+    const int ce = elem ? t % 3 : 0;          // component of the element
+    const int ie = it.sink0 + ke;
+    const int x = 3 * ie + ce;
+
+    double a = 0.0;
     if (it.nchunk > 1) {
-        if (owner) {
-            double* p = P.partial + 3 * ((long long)it.part_off + (long long)it.chunk * it.nsink + k);
-            p[0] = ax;
-            p[1] = ay;
-            p[2] = az;
+        // source chunks of one sink tile -> the CTA that finishes last reduces them
+        if (has && lane < 3) {
+            double* p = P.partial + 3 * ((long long)it.part_off + (long long)it.chunk * it.nsink) + 3 * k + lane;
+            *p = mine;
         }
         __threadfence();
         __syncthreads();
@@ -460,66 +453,131 @@ __global__ void __launch_bounds__(kTile) k_stage(const StageParams P)
         __syncthreads();
         if (!sm.last) return;   // uniform
         __threadfence();
-        // the lanes of each sink split the chunks (c = sub_lane, sub_lane + L, ...);
-        // loads are issued in batches so that they overlap, sums run in a fixed order
-        ax = ay = az = 0.0;
-        if (has) {
+        if (elem) {
+            // chunks in order, loads issued in batches of B
             constexpr int B = 8;
-            for (int c0 = sub_lane; c0 < it.nchunk; c0 += B * L) {
-                double px[B], py[B], pz[B];
+            const double* base = P.partial + 3 * (long long)it.part_off + t;
+            const long long stride = 3LL * it.nsink;
+            for (int c0 = 0; c0 < it.nchunk; c0 += B) {
+                double pv[B];
 #pragma unroll
-                for (int u = 0; u < B; u++) {
-                    const int c = c0 + u * L;
-                    if (c < it.nchunk) {
-                        const double* p = P.partial + 3 * ((long long)it.part_off + (long long)c * it.nsink + k);
-                        px[u] = __ldcg(p);
-                        py[u] = __ldcg(p + 1);
-                        pz[u] = __ldcg(p + 2);
-                    } else {
-                        px[u] = py[u] = pz[u] = 0.0;
-                    }
-                }
+                for (int u = 0; u < B; u++) pv[u] = (c0 + u < it.nchunk) ? __ldcg(base + (c0 + u) * stride) : 0.0;
 #pragma unroll
-                for (int u = 0; u < B; u++) {
-                    ax += px[u];
-                    ay += py[u];
-                    az += pz[u];
-                }
-            }
-        }
-        if (L > 1) {
-            __syncthreads();
-            sm.red[threadIdx.x][0] = ax;
-            sm.red[threadIdx.x][1] = ay;
-            sm.red[threadIdx.x][2] = az;
-            __syncthreads();
-            if (sub_lane == 0) {
-                for (int q = 1; q < L; q++) {
-                    ax += sm.red[k + q * SP][0];
-                    ay += sm.red[k + q * SP][1];
-                    az += sm.red[k + q * SP][2];
-                }
+                for (int u = 0; u < B; u++) a += pv[u];
             }
         }
         if (threadIdx.x == 0) P.tile_cnt[it.tile] = 0u;
+    } else {
+        if (has && lane < 3) sm.acc[3 * k + lane] = mine;
+        __syncthreads();
+        if (elem) a = sm.acc[t];
     }
 
-    double e = 0.0;
-    if (owner) e = stage_epilogue<MODE, EXACT>(P, it, S, i, ax, ay, az);
+    const SysInfo si = P.sinfo[it.sys];
+    const int s = P.stage;
+    const double dt = S->dt_try;
+    const bool drag_on = P.gas.enabled && it.cls == CLS_NSI;
+    double decr = 0.0;
+    if (drag_on) {
+        const double ts = P.standalone ? P.t_standalone
+                                       : S->t + (P.scheme == SCHEME_RKF78 ? c_tb.c[s] : c_tb.c4[s]) * dt;
+        decr = gas_reduction_factor(P.gas, ts);
+    }
+    const bool drag_act = drag_on && !(1.0e-6 > decr);
+    const bool star_term = (MODE == MODE_MIXED || MODE == MODE_FP32) && si.n_star > 0;
 
-    if (P.err_after) {
-        // CTA max of the error, one atomic per CTA (non-negative doubles order as their bits)
-        unsigned long long b = (unsigned long long)__double_as_longlong(e);
-        for (int o = 16; o > 0; o >>= 1) {
-            const unsigned long long ob = __shfl_xor_sync(0xffffffffu, b, o);
-            b = ob > b ? ob : b;
+    // scalars, one thread per sink: drag factor and gas velocity
+    if (drag_act && t < it.nsink) {
+        const int i = it.sink0 + t;
+        double f, gx, gy;
+        drag_factor(P.gas, decr, P.mass[si.off], P.r_in[3 * i], P.r_in[3 * i + 1], P.r_in[3 * i + 2],
+                    P.Kr[s][3 * i], P.Kr[s][3 * i + 1], P.Kr[s][3 * i + 2], P.cd[i], P.radius[i], P.density[i], f,
+                    gx, gy);
+        sm.sc[t][0] = f;
+        sm.sc[t][1] = gx;
+        sm.sc[t][2] = gy;
+    }
+    const double rc = elem ? P.r_in[x] : 0.0;
+    double sc_sum = 0.0;
+    if (star_term) {
+        // central-star term in FP64, m_j d / |d|^3 with |d|^-1 from rsqrt; the
+        // factor per (sink, star) is formed by one thread per sink
+        for (int j0 = si.off; j0 < si.off + si.n_star; j0 += kStarBatch) {
+            const int nst = min(kStarBatch, si.off + si.n_star - j0);
+            __syncthreads();
+            if (t < it.nsink) {
+                const int i = it.sink0 + t;
+                const double xi = P.r_in[3 * i], yi = P.r_in[3 * i + 1], zi = P.r_in[3 * i + 2];
+                for (int q = 0; q < nst; q++) {
+                    const int j = j0 + q;
+                    const double dx = P.r_in[3 * j] - xi, dy = P.r_in[3 * j + 1] - yi, dz = P.r_in[3 * j + 2] - zi;
+                    const double w = fma(dz, dz, fma(dy, dy, dx * dx));
+                    const double ri = rsqrt(w);
+                    sm.fs[t][q] = (j == i || P.id[j] < 0) ? 0.0 : P.mass[j] * (ri * ri) * ri;
+                }
+            }
+            __syncthreads();
+            if (elem)
+                for (int q = 0; q < nst; q++) sc_sum = fma(sm.fs[ke][q], P.r_in[3 * (j0 + q) + ce] - rc, sc_sum);
         }
-        if ((threadIdx.x & 31) == 0) sm.emax[threadIdx.x >> 5] = b;
+    } else {
         __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned long long m = 0;
-            for (int w = 0; w < kTile / 32; w++) m = sm.emax[w] > m ? sm.emax[w] : m;
-            if (m) atomicMax(&S->err_bits, m);
+    }
+    if (!elem) return;
+    if (star_term) a = sc_sum + a;
+    const int idi = P.id[ie];
+    if (!(idi > 0)) a = 0.0;   // calc_grav_accel_naive zeroes inactive sinks (pp_disk.cu:386-388)
+    if (drag_act) {
+        const double g = ce == 0 ? sm.sc[ke][1] : (ce == 1 ? sm.sc[ke][2] : 0.0);
+        a += sm.sc[ke][0] * (g - P.Kr[s][x]);
+    }
+    P.Kv[s][x] = a;
+    if (P.standalone) return;
+
+    if (P.next >= 0) {
+        double orr, ovv;
+        if (P.ynp1_to_out) {
+            const double b0 = mul<EXACT>(c_tb.b4[0], dt), b1 = mul<EXACT>(c_tb.b4[1], dt);
+            orr = rk4_ynp1<EXACT>(P.y_r[x], b0, b1, P.Kr[0][x], P.Kr[1][x], P.Kr[2][x], P.Kr[3][x]);
+            ovv = rk4_ynp1<EXACT>(P.y_v[x], b0, b1, P.Kv[0][x], P.Kv[1][x], P.Kv[2][x], P.Kv[3][x]);
+        } else {
+            combine<EXACT>(P, P.scheme, P.next, dt, x, orr, ovv);
+        }
+        P.r_out[x] = orr;
+        P.Kr[P.next][x] = ovv;
+        write_pos_c(P.pos_hi_out, P.pos_lo_out, ie, ce, orr);
+        if (ce == 0) {
+            reinterpret_cast<float*>(P.pos_hi_out + ie)[3] = __double2float_rn(idi >= 0 ? P.mass[ie] : 0.0);
+            reinterpret_cast<float*>(P.pos_lo_out + ie)[3] = __double2float_rn(P.radius[ie]);
+        }
+    }
+    if (P.err_after) {
+        double e = 0.0;
+        if (ie - si.off < si.n_err) {
+            double er, ev;
+            if (P.scheme == SCHEME_RKF78) {
+                // rk8_kernel::calc_error, int_rungekutta8.cu:248-260
+                er = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(P.Kr[0][x], P.Kr[10][x]), P.Kr[11][x]), P.Kr[12][x]));
+                ev = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(P.Kv[0][x], P.Kv[10][x]), P.Kv[11][x]), P.Kv[12][x]));
+            } else {
+                // rk4_kernel::calc_error, int_rungekutta4.cu:62-73
+                er = fabs(P.Kr[3][x] - P.Kr[4][x]);
+                ev = fabs(P.Kv[3][x] - P.Kv[4][x]);
+            }
+            e = fmax(er, ev);
+            if (er != er || ev != ev) e = __longlong_as_double(0x7ff8000000000000ll);
+        }
+        // max over the active lanes of the warp, one atomic per warp (non-negative
+        // doubles order as their bits; high words first, then low words)
+        const unsigned long long b = (unsigned long long)__double_as_longlong(e);
+        const unsigned m = __activemask();
+        const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+        const unsigned mh = __reduce_max_sync(m, hi);
+        const unsigned m2 = __ballot_sync(m, hi == mh);
+        if (hi == mh) {
+            const unsigned ml = __reduce_max_sync(m2, lo);
+            const unsigned long long w = ((unsigned long long)mh << 32) | ml;
+            if ((threadIdx.x & 31) == __ffs(m2) - 1 && w) atomicMax(&S->err_bits, w);
         }
     }
 }
@@ -585,53 +643,48 @@ __global__ void k_control(const ControlParams P)
     if (P.length != 0.0 && fabs(S.t - S.t_start) > fabs(P.length)) S.active = 0;
 }
 
+// y_{n+1} of the accepted systems and the positions of the next stage 0.  Four
+// threads per body: lanes 0..2 the x, y, z components, lane 3 the mass / radius
+// words of the FP32 copies.  Segments of kFinishBodies bodies.
 template <bool EXACT>
-__global__ void __launch_bounds__(kSegment) k_finish(const FinishParams P)
+__global__ void __launch_bounds__(4 * kFinishBodies) k_finish(const FinishParams P)
 {
     const Segment sg = P.segs[blockIdx.x];
     DevSys* S = P.sys + sg.sys;
     if (S->halted) return;
-    const int i = sg.b0 + threadIdx.x;
+    const int i = sg.b0 + threadIdx.x / 4;
+    const int c = threadIdx.x % 4;
     const bool acc = S->accepted;
     if (!acc && !runnable(*S)) return;
     if (i >= sg.b1) return;
-    double r[3], v[3];
+    if (c == 3) {
+        reinterpret_cast<float*>(P.pos_hi0 + i)[3] = __double2float_rn(P.id[i] >= 0 ? P.mass[i] : 0.0);
+        reinterpret_cast<float*>(P.pos_lo0 + i)[3] = __double2float_rn(P.radius[i]);
+        return;
+    }
+    const int x = 3 * i + c;
+    double r;
     if (acc) {
         const double dt = S->dt_did;
+        double v;
         if (P.scheme == SCHEME_RKF78) {
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                r[c] = rk8_ynp1<EXACT>(P.y_r[3 * i + c], dt, P.Kr, 3 * i + c);
-                v[c] = rk8_ynp1<EXACT>(P.y_v[3 * i + c], dt, P.Kv, 3 * i + c);
-            }
+            r = rk8_ynp1<EXACT>(P.y_r[x], dt, P.Kr, x);
+            v = rk8_ynp1<EXACT>(P.y_v[x], dt, P.Kv, x);
         } else if (P.commit_from_stage4) {
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                r[c] = P.t_r0[3 * i + c];
-                v[c] = P.Kr[4][3 * i + c];
-            }
+            r = P.t_r0[x];
+            v = P.Kr[4][x];
         } else {
             const double b0 = mul<EXACT>(c_tb.b4[0], dt), b1 = mul<EXACT>(c_tb.b4[1], dt);
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                const int x = 3 * i + c;
-                r[c] = rk4_ynp1<EXACT>(P.y_r[x], b0, b1, P.Kr[0][x], P.Kr[1][x], P.Kr[2][x], P.Kr[3][x]);
-                v[c] = rk4_ynp1<EXACT>(P.y_v[x], b0, b1, P.Kv[0][x], P.Kv[1][x], P.Kv[2][x], P.Kv[3][x]);
-            }
+            r = rk4_ynp1<EXACT>(P.y_r[x], b0, b1, P.Kr[0][x], P.Kr[1][x], P.Kr[2][x], P.Kr[3][x]);
+            v = rk4_ynp1<EXACT>(P.y_v[x], b0, b1, P.Kv[0][x], P.Kv[1][x], P.Kv[2][x], P.Kv[3][x]);
         }
-        bool fin = true;
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            P.y_r[3 * i + c] = r[c];
-            P.y_v[3 * i + c] = v[c];
-            fin = fin && isfinite(r[c]) && isfinite(v[c]);
-        }
-        if (!fin) S->status = 5;
+        P.y_r[x] = r;
+        P.y_v[x] = v;
+        if (!(isfinite(r) && isfinite(v))) S->status = 5;   // RED_ERR_NONFINITE
     } else {
-#pragma unroll
-        for (int c = 0; c < 3; c++) r[c] = P.y_r[3 * i + c];
+        r = P.y_r[x];
     }
-    write_pos(P.pos_hi0, P.pos_lo0, i, r[0], r[1], r[2], P.id[i] >= 0 ? P.mass[i] : 0.0, P.radius[i]);
+    write_pos_c(P.pos_hi0, P.pos_lo0, i, c, r);
 }
 
 // ---------------------------------------------------------------------------
@@ -639,66 +692,156 @@ __global__ void __launch_bounds__(kSegment) k_finish(const FinishParams P)
 // over tile pairs; an FP32 double-single prefilter with a safety margin picks
 // the candidates, red's FP64 test (no FMA) decides.
 // ---------------------------------------------------------------------------
+// After a try the check runs for the systems that just accepted one (a halted
+// system makes no tries, so it never has `accepted` set); the explicit check
+// runs for every system.  `halted` is not consulted: the first kernel of the
+// check may set it.
+__device__ __forceinline__ bool coll_runs(const CollParams& P, const DevSys& S)
+{
+    return !P.only_accepted || S.accepted;
+}
+
+// red's test for one pair i < j, bit for bit (pp_disk.cu:336-357), and the event.
+__device__ __forceinline__ void collide_exact(const CollParams& P, DevSys* S, int sys, int i, int jx, double f)
+{
+    if (!(0 < P.id[i]) || 0 > P.id[jx]) return;
+    const double ddx = __dsub_rn(P.y_r[3 * jx], P.y_r[3 * i]);
+    const double ddy = __dsub_rn(P.y_r[3 * jx + 1], P.y_r[3 * i + 1]);
+    const double ddz = __dsub_rn(P.y_r[3 * jx + 2], P.y_r[3 * i + 2]);
+    const double w = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
+    const double rs = __dadd_rn(P.radius[i], P.radius[jx]);
+    if (!(w < __dmul_rn(f, __dmul_rn(rs, rs)))) return;
+    int surv = i, merg = jx;
+    if (P.mass[merg] > P.mass[surv]) {
+        surv = jx;
+        merg = i;
+    }
+    const unsigned kk = atomicAdd(P.n_events, 1u);
+    if (kk < P.capacity) {
+        DevEvent ev;
+        ev.sys = sys;
+        ev.name = 3;   // RED_EVENT_COLLISION
+        ev.i = i;
+        ev.j = jx;
+        ev.surv = surv;
+        ev.merg = merg;
+        ev.d = __dsqrt_rn(w);
+        P.events[kk] = ev;
+    }
+    if (P.mark) {
+        atomicAdd(&S->n_coll, 1);
+        S->halted = 1;
+    }
+}
+
+// Brute-force tile pairs: the large bodies (SI class) against every later body.
+// One thread per later body j; the i tile (the SI bodies) sits in shared
+// memory.  FP32 double-single prefilter with a safety margin, red's FP64
+// test decides.
 __global__ void __launch_bounds__(kTile) k_collision(const CollParams P)
 {
     __shared__ float4 shi[kTile], slo[kTile];
     const PairItem it = P.items[blockIdx.x];
     DevSys* S = P.sys + it.sys;
-    if (S->halted) return;
-    if (P.only_accepted && !S->accepted) return;
+    if (!coll_runs(P, *S)) return;
     const SysInfo si = P.sinfo[it.sys];
     const int end = si.off + si.n;
-    const int i = it.i0 + threadIdx.x;
-    const int j = it.j0 + threadIdx.x;
-    if (j < end) {
-        shi[threadIdx.x] = P.pos_hi[j];
-        slo[threadIdx.x] = P.pos_lo[j];
+    const int ni = min(kTile, it.i1 - it.i0);
+    if (threadIdx.x < ni) {
+        shi[threadIdx.x] = P.pos_hi[it.i0 + threadIdx.x];
+        slo[threadIdx.x] = P.pos_lo[it.i0 + threadIdx.x];
     }
     __syncthreads();
-    if (i >= end) return;
-    const float4 H = P.pos_hi[i], Lo = P.pos_lo[i];
-    const int nj = min(kTile, end - it.j0);
+    const int j = it.j0 + threadIdx.x;
+    if (j >= end) return;
+    const float4 H = P.pos_hi[j], Lo = P.pos_lo[j];
     const float fac = (float)P.factor;
     const double f = P.factor * P.factor;
-    for (int jj = 0; jj < nj; jj++) {
-        const int jx = it.j0 + jj;
-        if (jx <= i) continue;
-        const float4 h = shi[jj], l = slo[jj];
-        const float dx = (h.x - H.x) + (l.x - Lo.x);
-        const float dy = (h.y - H.y) + (l.y - Lo.y);
-        const float dz = (h.z - H.z) + (l.z - Lo.z);
+    const int nii = min(ni, j - it.i0);   // i < j
+    for (int ii = 0; ii < nii; ii++) {
+        const float4 h = shi[ii], l = slo[ii];
+        const float dx = (H.x - h.x) + (Lo.x - l.x);
+        const float dy = (H.y - h.y) + (Lo.y - l.y);
+        const float dz = (H.z - h.z) + (Lo.z - l.z);
         const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         const float th = fac * (Lo.w + l.w);
         if (!(d2 <= 1.0001f * th * th + 1.0e-30f)) continue;
-        // red's test, bit for bit (pp_disk.cu:336-357)
-        if (!(0 < P.id[i]) || 0 > P.id[jx]) continue;
-        const double ddx = __dsub_rn(P.y_r[3 * jx], P.y_r[3 * i]);
-        const double ddy = __dsub_rn(P.y_r[3 * jx + 1], P.y_r[3 * i + 1]);
-        const double ddz = __dsub_rn(P.y_r[3 * jx + 2], P.y_r[3 * i + 2]);
-        const double w = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
-        const double rs = __dadd_rn(P.radius[i], P.radius[jx]);
-        if (w < __dmul_rn(f, __dmul_rn(rs, rs))) {
-            int surv = i, merg = jx;
-            if (P.mass[merg] > P.mass[surv]) {
-                surv = jx;
-                merg = i;
+        collide_exact(P, S, it.sys, it.i0 + ii, j, f);
+    }
+}
+
+// Spatial-hash broad phase for the small bodies.  Cell coordinates are
+// clamped so that far-away bodies share border cells (tested exactly, never
+// missed).
+__device__ __forceinline__ int4 cell_of(double x, double y, double z, double inv_h)
+{
+    const double lim = 1.0e9;
+    int4 c;
+    c.x = (int)floor(fmin(fmax(x * inv_h, -lim), lim));
+    c.y = (int)floor(fmin(fmax(y * inv_h, -lim), lim));
+    c.z = (int)floor(fmin(fmax(z * inv_h, -lim), lim));
+    c.w = 0;
+    return c;
+}
+
+__device__ __forceinline__ int bucket_of(int cx, int cy, int cz, int mask)
+{
+    const unsigned h = ((unsigned)cx * 73856093u) ^ ((unsigned)cy * 19349663u) ^ ((unsigned)cz * 83492791u);
+    return (int)(h & (unsigned)mask);
+}
+
+__global__ void __launch_bounds__(kSegment) k_grid_insert(const CollParams P)
+{
+    const Segment sg = P.segs[blockIdx.x];
+    const DevSys& S = P.sys[sg.sys];
+    const GridInfo g = P.grid[sg.sys];
+    if (!g.enabled || !coll_runs(P, S)) return;
+    const SysInfo si = P.sinfo[sg.sys];
+    const int i = sg.b0 + threadIdx.x;
+    if (i >= sg.b1 || i < si.off + si.n_SI) return;
+    const int4 c = cell_of(P.y_r[3 * i], P.y_r[3 * i + 1], P.y_r[3 * i + 2], g.inv_h);
+    P.cell[i] = c;
+    P.next[i] = atomicExch(&P.head[g.toff + bucket_of(c.x, c.y, c.z, g.mask)], i);
+}
+
+// Half of the neighbourhood: the own cell (pairs with j > i) and the 13 cells
+// of the forward half-space, so that every unordered pair of small bodies in
+// neighbouring cells is seen once; the pair is tested as (min, max) like red's
+// i < j loop.  The 14 bucket heads are loaded before any list is walked.
+__global__ void __launch_bounds__(kSegment) k_grid_query(const CollParams P)
+{
+    const Segment sg = P.segs[blockIdx.x];
+    DevSys* S = P.sys + sg.sys;
+    const GridInfo g = P.grid[sg.sys];
+    if (!g.enabled || !coll_runs(P, *S)) return;
+    const SysInfo si = P.sinfo[sg.sys];
+    const int i = sg.b0 + threadIdx.x;
+    if (i >= sg.b1 || i < si.off + si.n_SI) return;
+    const double f = P.factor * P.factor;
+    const int4 c = P.cell[i];
+    int head[14];
+    int4 nb[14];
+    int q = 0;
+#pragma unroll
+    for (int dz = 0; dz <= 1; dz++)
+#pragma unroll
+        for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+            for (int dx = -1; dx <= 1; dx++) {
+                const bool fwd = dz > 0 || (dz == 0 && (dy > 0 || (dy == 0 && dx >= 0)));
+                if (!fwd) continue;
+                nb[q] = make_int4(c.x + dx, c.y + dy, c.z + dz, 0);
+                head[q] = __ldcg(P.head + g.toff + bucket_of(nb[q].x, nb[q].y, nb[q].z, g.mask));
+                q++;
             }
-            const unsigned kk = atomicAdd(P.n_events, 1u);
-            if (kk < P.capacity) {
-                DevEvent ev;
-                ev.sys = it.sys;
-                ev.name = 3;   // RED_EVENT_COLLISION
-                ev.i = i;
-                ev.j = jx;
-                ev.surv = surv;
-                ev.merg = merg;
-                ev.d = __dsqrt_rn(w);
-                P.events[kk] = ev;
-            }
-            if (P.mark) {
-                atomicAdd(&S->n_coll, 1);
-                S->halted = 1;
-            }
+#pragma unroll
+    for (int b = 0; b < 14; b++) {
+        int j = head[b];
+        while (j >= 0) {
+            const int4 cj = P.cell[j];
+            if (cj.x == nb[b].x && cj.y == nb[b].y && cj.z == nb[b].z && (b != 0 || j > i))
+                collide_exact(P, S, sg.sys, min(i, j), max(i, j), f);
+            j = __ldcg(P.next + j);
         }
     }
 }
@@ -812,13 +955,19 @@ void launch_control(const ControlParams& P, cudaStream_t s)
 void launch_finish(const FinishParams& P, int n_segs, cudaStream_t s)
 {
     if (n_segs <= 0) return;
-    if (P.stage_exact) k_finish<true><<<n_segs, kSegment, 0, s>>>(P);
-    else k_finish<false><<<n_segs, kSegment, 0, s>>>(P);
+    if (P.stage_exact) k_finish<true><<<n_segs, 4 * kFinishBodies, 0, s>>>(P);
+    else k_finish<false><<<n_segs, 4 * kFinishBodies, 0, s>>>(P);
 }
 
-void launch_collision(const CollParams& P, int n_items, cudaStream_t s)
+void launch_collision(const CollParams& P, int n_items, int n_segs, bool use_grid, size_t table_size,
+                      cudaStream_t s)
 {
     if (n_items > 0) k_collision<<<n_items, kTile, 0, s>>>(P);
+    if (use_grid && n_segs > 0) {
+        cudaMemsetAsync(P.head, 0xff, table_size * sizeof(int), s);
+        k_grid_insert<<<n_segs, kSegment, 0, s>>>(P);
+        k_grid_query<<<n_segs, kSegment, 0, s>>>(P);
+    }
 }
 
 void launch_ejhc(const EjhcParams& P, int n_segs, cudaStream_t s)

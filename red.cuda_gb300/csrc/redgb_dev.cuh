@@ -18,6 +18,7 @@ namespace redgb {
 
 constexpr int kTile = 128;          // sinks per CTA and sources per shared-memory tile
 constexpr int kSegment = 256;       // bodies per CTA in the per-body kernels
+constexpr int kFinishBodies = 64;   // bodies per CTA of k_finish (four threads each)
 constexpr int kMaxStages = 13;
 
 enum Mode { MODE_MIXED = 0, MODE_FP64 = 1, MODE_FP64_EXACT = 2, MODE_FP32 = 3 };
@@ -65,7 +66,7 @@ struct GravItem {
     int chunk, nchunk;
     int tile;             // tile id: counter index when nchunk > 1
     int part_off;         // first partial record of the tile
-    int lanes;            // threads per sink, lanes * nsink <= kTile
+    int lanes;            // threads per sink (4, 8, 16 or 32), lanes * nsink <= kTile
     int cls;
     int pad;
 };
@@ -75,9 +76,20 @@ struct Segment {
     int sys, b0, b1, pad;
 };
 
-// Tile pair of the collision check (I <= J, tiles of kTile bodies of one system).
+// Tile pair of the brute-force collision check: i in [i0, min(i0 + kTile, i1)),
+// j in the tile starting at j0, j > i (bodies of one system).
 struct PairItem {
-    int sys, i0, j0, pad;
+    int sys, i0, j0, i1;
+};
+
+// Spatial hash grid of one system's small bodies (the NSI and NI classes) for
+// the collision check: cells of edge 1/inv_h >= the largest collision distance
+// between two small bodies, buckets [toff, toff + mask + 1) of a global table.
+struct GridInfo {
+    double inv_h;
+    int toff, mask;
+    int enabled;
+    int pad;
 };
 
 // Compact collision / ejection record written by the device.
@@ -168,6 +180,11 @@ struct ControlParams {
 
 struct CollParams {
     const PairItem* items;
+    const Segment* segs;
+    const GridInfo* grid;
+    int* head;            // bucket heads (-1 = empty)
+    int* next;            // per-body link of the bucket lists
+    int4* cell;           // per-body cell coordinates
     const SysInfo* sinfo;
     DevSys* sys;
     const float4* pos_hi;
@@ -207,7 +224,8 @@ void launch_prep(const Segment* segs, int n_segs, const SysInfo* sinfo, const De
                  cudaStream_t s);
 void launch_control(const ControlParams& P, cudaStream_t s);
 void launch_finish(const FinishParams& P, int n_segs, cudaStream_t s);
-void launch_collision(const CollParams& P, int n_items, cudaStream_t s);
+void launch_collision(const CollParams& P, int n_items, int n_segs, bool use_grid, size_t table_size,
+                      cudaStream_t s);
 void launch_ejhc(const EjhcParams& P, int n_segs, cudaStream_t s);
 void launch_potential(const Segment* segs, int n_segs, const SysInfo* sinfo, const double* y_r,
                       const double* mass, const int* id, int sys_filter, int interacting, double* u,

@@ -171,8 +171,17 @@ struct red_sim {
     size_t items_cap = 0;
     Segment* d_segs = nullptr;
     size_t segs_cap = 0;
+    Segment* d_fsegs = nullptr;
+    size_t fsegs_cap = 0;
     PairItem* d_pairs = nullptr;
     size_t pairs_cap = 0;
+    GridInfo* d_grid = nullptr;
+    int* d_head = nullptr;
+    size_t head_cap = 0;
+    size_t table_size = 0;
+    int* d_next = nullptr;
+    int4* d_cell = nullptr;
+    bool use_grid = false;
     DevEvent* d_events = nullptr;
     unsigned int* d_nev = nullptr;
     uint32_t ev_cap = 0;
@@ -181,10 +190,12 @@ struct red_sim {
     // plan
     std::vector<GravItem> items;
     std::vector<Segment> segs;
+    std::vector<Segment> fsegs;   // kFinishBodies bodies each (k_finish)
     std::vector<PairItem> pairs;
     std::vector<SysInfo> sinfo;
+    std::vector<GridInfo> grid;
     int chunk_override = 0;     // sources per chunk chosen by the autotuner (0 = heuristic)
-    int lanes_cap = 128;        // upper bound on threads per sink (autotuner)
+    int lanes_cap = 32;         // upper bound on threads per sink (autotuner)
 
     cudaGraphExec_t graph = nullptr;
     int launches_per_try = 0;
@@ -210,6 +221,38 @@ struct red_sim {
     int handle_events(red_event_t* out, uint32_t cap, uint32_t* n_out);
     void rebuild_system(uint32_t s);
     void invalidate() { if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; } }
+    bool has_ejhc() const
+    {
+        return cfg.threshold[RED_THRESHOLD_EJECTION_DISTANCE] > 0.0 ||
+               cfg.threshold[RED_THRESHOLD_HIT_CENTRUM_DISTANCE] > 0.0;
+    }
+    bool ejhc_initial_done = false;
+    // Ejection / hit-centrum check of every system's current state, halting the
+    // systems with events (run_simulation checks before every step, main.cu:499-523).
+    void ejhc_all()
+    {
+        EjhcParams E;
+        memset(&E, 0, sizeof(E));
+        E.segs = d_segs; E.sinfo = d_sinfo; E.sys = d_sys; E.y_r = y_r; E.id = id; E.btype = btype;
+        E.ejection = cfg.threshold[RED_THRESHOLD_EJECTION_DISTANCE];
+        E.hit_centrum = cfg.threshold[RED_THRESHOLD_HIT_CENTRUM_DISTANCE];
+        E.only_accepted = 0;
+        E.mark = 1;
+        E.events = d_events; E.n_events = d_nev; E.capacity = ev_cap;
+        launch_ejhc(E, (int)segs.size(), stream);
+        CK(cudaGetLastError());
+        launches++;
+    }
+    void fill_coll(CollParams& Q)
+    {
+        memset(&Q, 0, sizeof(Q));
+        Q.items = d_pairs; Q.segs = d_segs; Q.grid = d_grid; Q.head = d_head; Q.next = d_next; Q.cell = d_cell;
+        Q.sinfo = d_sinfo; Q.sys = d_sys;
+        Q.pos_hi = pos_hi[0]; Q.pos_lo = pos_lo[0]; Q.y_r = y_r;
+        Q.radius = radius; Q.mass = mass; Q.id = id;
+        Q.factor = cfg.threshold[RED_THRESHOLD_RADII_ENHANCE_FACTOR];
+        Q.events = d_events; Q.n_events = d_nev; Q.capacity = ev_cap;
+    }
     uint64_t interactions_per_eval() const;
 };
 
@@ -223,6 +266,7 @@ red_sim::~red_sim()
     cudaFree(mass); cudaFree(radius); cudaFree(density); cudaFree(cd); cudaFree(id); cudaFree(btype);
     cudaFree(partial); cudaFree(tile_cnt); cudaFree(d_sys); cudaFree(d_sinfo); cudaFree(d_items);
     cudaFree(d_segs); cudaFree(d_pairs); cudaFree(d_events); cudaFree(d_nev); cudaFree(d_u);
+    cudaFree(d_grid); cudaFree(d_head); cudaFree(d_next); cudaFree(d_cell); cudaFree(d_fsegs);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -323,6 +367,9 @@ void red_sim::create(const red_config_t* c, uint32_t n_systems, const uint32_t* 
     mass = dalloc<double>(N); radius = dalloc<double>(N); density = dalloc<double>(N); cd = dalloc<double>(N);
     id = dalloc<int>(N); btype = dalloc<int>(N);
     d_u = dalloc<double>(N);
+    d_next = dalloc<int>(N);
+    d_cell = dalloc<int4>(N);
+    d_grid = dalloc<GridInfo>(n_sys);
     CK(cudaMemcpy(y_r, hr.data(), 3 * N * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(y_v, hv.data(), 3 * N * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(mass, hm.data(), N * sizeof(double), cudaMemcpyHostToDevice));
@@ -359,8 +406,14 @@ void red_sim::build_plan()
     invalidate();
     items.clear();
     segs.clear();
+    fsegs.clear();
     pairs.clear();
     sinfo.assign(n_sys, SysInfo{});
+    grid.assign(n_sys, GridInfo{});
+    size_t table = 0;
+    // radii, for the cell size of the collision grid
+    std::vector<double> h_radius(n_cap);
+    CK(cudaMemcpy(h_radius.data(), radius, n_cap * sizeof(double), cudaMemcpyDeviceToHost));
     size_t part = 0;
     int tiles = 0;
     const bool fp32 = (mode == MODE_MIXED || mode == MODE_FP32);
@@ -383,15 +436,17 @@ void red_sim::build_plan()
             const int nsink_all = q.s1 - q.s0;
             if (nsink_all <= 0) continue;
             const int nsrc = std::max(0, q.j1 - q.j0);
-            const int ntile = (nsink_all + kTile - 1) / kTile;
+            // threads per sink: a power of two in [4, 32]; few sinks get more lanes
+            int lanes = 4;
+            if (mode != MODE_FP64_EXACT)
+                while (lanes < 32 && lanes < lanes_cap && 2 * lanes * nsink_all <= kTile) lanes *= 2;
+            const int tile_sinks = kTile / lanes;
+            const int ntile = (nsink_all + tile_sinks - 1) / tile_sinks;
             for (int t = 0; t < ntile; t++) {
-                const int s0 = q.s0 + t * kTile;
-                const int nsink = std::min(kTile, q.s1 - s0);
-                int lanes = 1;
+                const int s0 = q.s0 + t * tile_sinks;
+                const int nsink = std::min(tile_sinks, q.s1 - s0);
                 int chunk = std::max(nsrc, 1);
                 if (mode != MODE_FP64_EXACT) {
-                    // few sinks: several threads per sink over interleaved sources
-                    lanes = std::max(1, std::min(std::min(kTile / nsink, lanes_cap), std::max(1, nsrc)));
                     int c;
                     if (chunk_override > 0) {
                         c = chunk_override;
@@ -428,9 +483,34 @@ void red_sim::build_plan()
             }
         }
         for (int b = 0; b < si.n; b += kSegment) segs.push_back(Segment{(int)s, si.off + b, si.off + std::min(si.n, b + kSegment), 0});
+        for (int b = 0; b < si.n; b += kFinishBodies)
+            fsegs.push_back(Segment{(int)s, si.off + b, si.off + std::min(si.n, b + kFinishBodies), 0});
+        // collision check: the SI bodies (large radii) by brute force against
+        // every later body, the rest through the spatial hash grid
         const int T = (si.n + kTile - 1) / kTile;
-        for (int I = 0; I < T; I++)
-            for (int J = I; J < T; J++) pairs.push_back(PairItem{(int)s, si.off + I * kTile, si.off + J * kTile, 0});
+        const int TI = (si.n_SI + kTile - 1) / kTile;
+        for (int I = 0; I < TI; I++)
+            for (int J = I; J < T; J++)
+                pairs.push_back(PairItem{(int)s, si.off + I * kTile, si.off + J * kTile, si.off + si.n_SI});
+        GridInfo& g = grid[s];
+        memset(&g, 0, sizeof(g));
+        const int n_small = si.n - si.n_SI;
+        double rmax = 0.0;
+        for (int k = si.n_SI; k < si.n; k++) rmax = std::max(rmax, h_radius[si.off + k]);
+        const double factor = cfg.threshold[RED_THRESHOLD_RADII_ENHANCE_FACTOR];
+        if (n_small > 1 && rmax > 0.0 && factor > 0.0) {
+            // cell edge >= the largest collision distance f (R_i + R_j) of two small
+            // bodies, widened a little so that rounding in x / h cannot split a pair
+            // by more than one cell
+            const double h = 2.0 * factor * rmax * (1.0 + 1.0e-6) + 1.0e-300;
+            size_t m = 1024;
+            while (m < 2 * (size_t)n_small) m <<= 1;
+            g.inv_h = 1.0 / h;
+            g.toff = (int)table;
+            g.mask = (int)(m - 1);
+            g.enabled = 1;
+            table += m;
+        }
     }
     auto upload = [&](auto& vec, auto*& dptr, size_t& cap) {
         using T = typename std::remove_reference<decltype(vec)>::type::value_type;
@@ -443,8 +523,17 @@ void red_sim::build_plan()
     };
     upload(items, d_items, items_cap);
     upload(segs, d_segs, segs_cap);
+    upload(fsegs, d_fsegs, fsegs_cap);
     upload(pairs, d_pairs, pairs_cap);
     CK(cudaMemcpy(d_sinfo, sinfo.data(), n_sys * sizeof(SysInfo), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_grid, grid.data(), n_sys * sizeof(GridInfo), cudaMemcpyHostToDevice));
+    table_size = table;
+    use_grid = table > 0;
+    if (table > head_cap) {
+        cudaFree(d_head);
+        head_cap = table;
+        d_head = dalloc<int>(head_cap);
+    }
     if (part > partial_cap) {
         cudaFree(partial);
         partial_cap = part;
@@ -554,7 +643,7 @@ void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs
     F.adaptive = cfg.adaptive;
     F.commit_from_stage4 = (scheme == SCHEME_RK4 && cfg.adaptive) ? 1 : 0;
     F.stage_exact = cfg.stage_exact;
-    F.segs = d_segs;
+    F.segs = d_fsegs;
     F.sinfo = d_sinfo;
     F.sys = d_sys;
     F.y_r = y_r;
@@ -569,20 +658,16 @@ void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs
     F.id = id;
     F.pos_hi0 = pos_hi[0];
     F.pos_lo0 = pos_lo[0];
-    launch_finish(F, (int)segs.size(), stream);
+    launch_finish(F, (int)fsegs.size(), stream);
     mark(2);
     n++;
     if (cfg.threshold[RED_THRESHOLD_RADII_ENHANCE_FACTOR] > 0.0) {
         CollParams Q;
         memset(&Q, 0, sizeof(Q));
-        Q.items = d_pairs; Q.sinfo = d_sinfo; Q.sys = d_sys;
-        Q.pos_hi = pos_hi[0]; Q.pos_lo = pos_lo[0]; Q.y_r = y_r;
-        Q.radius = radius; Q.mass = mass; Q.id = id;
-        Q.factor = cfg.threshold[RED_THRESHOLD_RADII_ENHANCE_FACTOR];
+        fill_coll(Q);
         Q.only_accepted = 1;
         Q.mark = 1;
-        Q.events = d_events; Q.n_events = d_nev; Q.capacity = ev_cap;
-        launch_collision(Q, (int)pairs.size(), stream);
+        launch_collision(Q, (int)pairs.size(), (int)segs.size(), use_grid, table_size, stream);
         mark(3);
         n++;
     }
@@ -620,6 +705,10 @@ void red_sim::capture()
 
 void red_sim::launch_tries(uint32_t n)
 {
+    if (has_ejhc() && !ejhc_initial_done) {
+        ejhc_initial_done = true;
+        ejhc_all();
+    }
     capture();
     for (uint32_t k = 0; k < n; k++) {
         CK(cudaGraphLaunch(graph, stream));
@@ -876,6 +965,21 @@ int red_sim::handle_events(red_event_t* out, uint32_t cap, uint32_t* n_out)
         build_plan();
         prep_positions();
         CK(cudaStreamSynchronize(stream));
+        // systems whose ejection check was skipped because of collisions get it now
+        // (red checks at the start of the next loop iteration, main.cu:499-523)
+        if (has_ejhc() && rc == RED_OK) {
+            ejhc_all();
+            std::vector<DevSys> d2;
+            read_sys(d2);
+            bool again = false;
+            for (const DevSys& d : d2) again = again || d.halted;
+            if (again) {
+                uint32_t more = 0;
+                const uint32_t room = (out && cap > n_written) ? cap - n_written : 0;
+                rc = handle_events(out ? out + std::min(n_written, cap) : nullptr, room, &more);
+                n_written += more;
+            }
+        }
     }
     if (n_out) *n_out = n_written;
     return rc;
@@ -1043,15 +1147,12 @@ static int check_generic(red_sim* sim, int collision, red_event_t* out, uint32_t
     if (collision) {
         CollParams Q;
         memset(&Q, 0, sizeof(Q));
-        Q.items = sim->d_pairs; Q.sinfo = sim->d_sinfo; Q.sys = sim->d_sys;
-        Q.pos_hi = sim->pos_hi[0]; Q.pos_lo = sim->pos_lo[0]; Q.y_r = sim->y_r;
-        Q.radius = sim->radius; Q.mass = sim->mass; Q.id = sim->id;
-        Q.factor = sim->cfg.threshold[RED_THRESHOLD_RADII_ENHANCE_FACTOR];
+        sim->fill_coll(Q);
         Q.only_accepted = 0;
         Q.mark = 0;
-        Q.events = sim->d_events; Q.n_events = sim->d_nev; Q.capacity = sim->ev_cap;
         sim->prep_positions();
-        launch_collision(Q, (int)sim->pairs.size(), sim->stream);
+        launch_collision(Q, (int)sim->pairs.size(), (int)sim->segs.size(), sim->use_grid, sim->table_size,
+                         sim->stream);
     } else {
         EjhcParams E;
         memset(&E, 0, sizeof(E));

@@ -301,3 +301,27 @@ def test_ensemble_equals_single_systems(rg):
             st = sim.get_state(k)
             assert sim.info(k).t == singles[k][1]
             assert np.array_equal(vec(st.r), vec(singles[k][0].r))
+
+
+@pytest.mark.parametrize("factor", [300.0, 2000.0])
+def test_collision_many_pairs_grid(rg, orc, factor):
+    # enlarged radii make many planetesimal pairs overlap: the spatial-hash grid
+    # (small bodies) and the brute-force pass (SI bodies) must find red's exact pair set
+    systems = [rg.ic.config1(seed=31 + k, n_pl=1500 + 500 * k) for k in range(3)]
+    with rg.Sim(systems, dt=0.01, collision_factor=factor, event_capacity=1 << 16) as sim:
+        ev = sim.check_for_collision(cap=1 << 16)
+    got = {}
+    for e in ev:
+        got.setdefault(len(got), None)
+    n_ref = 0
+    start = 0
+    for k, s in enumerate(systems):
+        _, ref, n = orc.check_collision(obody(orc, s), 0.0, factor, sem=orc.SEM_GPU, cap=1 << 16)
+        assert n == len(ref)
+        n_ref += n
+        mine = ev[start:start + n]
+        start += n
+        assert keys(mine) == keys(ref), k
+        assert np.array_equal(mine["d"], ref["d"])
+    assert len(ev) == n_ref
+    assert n_ref > 50
