@@ -199,6 +199,37 @@ uint64_t red_interactions_per_eval(red_sim* sim);
 uint64_t red_kernel_launches(red_sim* sim);
 uint32_t red_n_systems(red_sim* sim);
 
+/* ---- allocation-free gravity ---------------------------------------------
+ * No counterpart in red.  For callers that cannot call cudaMalloc (device
+ * memory owned by another pool, real-time loops that must not enter the
+ * allocator): gravity plus analytic drag of one system, as red_calc_dydx with
+ * i = 1, from device buffers the caller owns, launched on the caller's
+ * stream.  Temporaries live in a fixed 4 MiB __device__ array inside the
+ * library, held by every GPU that loads it until exit; calls share it, so
+ * calls that overlap on the GPU race and must be ordered by the caller.  The
+ * first call on a device looks the array up and loads constant tables: make
+ * it before any stream capture.  Systems above RED_NOALLOC_MAX_BODIES bodies
+ * are rejected with RED_ERR_ARG. */
+#define RED_NOALLOC_MAX_BODIES 32768
+typedef struct {
+    uint32_t playing[RED_BODY_N];  /* bodies per type; bodies sorted by type */
+    const double* r;               /* device: x, y, z per body (3 N doubles) */
+    const double* v;               /* device: velocities (3 N), needed with gas drag */
+    const double* mass;            /* device: N doubles */
+    const double* radius;          /* device: N doubles (may be NULL without gas drag) */
+    const double* density;         /* device: N doubles (gas drag) */
+    const double* cd;              /* device: N doubles (gas drag) */
+    const int32_t* id;             /* device: N body ids (id < 0: inactive) */
+    double* accel;                 /* device: output accelerations (3 N doubles) */
+    int32_t precision;             /* RED_PREC_* */
+    int32_t gas_disk;              /* 0 none, 1 analytic */
+    red_gas_params_t gas;
+    double t;                      /* time of the evaluation (gas density factor) */
+    int32_t device;                /* CUDA device ordinal */
+    void* stream;                  /* cudaStream_t; NULL = legacy default stream */
+} red_accel_args_t;
+int red_calc_accel_noalloc(const red_accel_args_t* args);
+
 const char* red_last_error(void);
 const char* red_version(void);
 

@@ -12,6 +12,7 @@
 // The .w lane red integrates (always 0) is not stored.
 #pragma once
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 namespace redgb {
@@ -215,6 +216,10 @@ struct EjhcParams {
     unsigned int* n_events;
     unsigned int capacity;
 };
+
+// Host-side plan of the stage kernel for one system (sim.cu).
+void plan_gravity_items(const SysInfo& si, int sys, int mode, int chunk_override, int lanes_cap,
+                        std::vector<GravItem>& items, size_t& part, int& tiles);
 
 // Host-side launchers (kernels.cu).
 void set_tableau(const Tableau& tb, cudaStream_t s);

@@ -138,6 +138,74 @@ struct HostState {
 
 }  // namespace
 
+
+namespace redgb {
+// CTAs of the stage kernel for one system: sink tiles of the SI, NSI and NI
+// classes (red_type.h:670-692), each split into source chunks; appends to
+// items and advances the partial-record and tile counters.
+void plan_gravity_items(const SysInfo& si, int s, int mode, int chunk_override, int lanes_cap,
+                        std::vector<GravItem>& items, size_t& part, int& tiles)
+{
+    const int kTargetCtas = 8 * 152;   // ~8 resident CTAs on each of GB300's 152 SMs
+    const bool fp32 = (mode == MODE_MIXED || mode == MODE_FP32);
+        const int src_start = fp32 ? si.n_star : 0;
+        struct C { int cls, s0, s1, j0, j1; };
+        const C cls[3] = {{CLS_SI, 0, si.n_SI, src_start, si.n_massive},
+                          {CLS_NSI, si.n_SI, si.n_massive, src_start, si.n_SI},
+                          {CLS_NI, si.n_massive, si.n, src_start, si.n_massive}};
+        for (const C& q : cls) {
+            const int nsink_all = q.s1 - q.s0;
+            if (nsink_all <= 0) continue;
+            const int nsrc = std::max(0, q.j1 - q.j0);
+            // threads per sink: a power of two in [4, 32]; few sinks get more lanes
+            int lanes = 4;
+            if (mode != MODE_FP64_EXACT)
+                while (lanes < 32 && lanes < lanes_cap && 2 * lanes * nsink_all <= kTile) lanes *= 2;
+            const int tile_sinks = kTile / lanes;
+            const int ntile = (nsink_all + tile_sinks - 1) / tile_sinks;
+            for (int t = 0; t < ntile; t++) {
+                const int s0 = q.s0 + t * tile_sinks;
+                const int nsink = std::min(tile_sinks, q.s1 - s0);
+                int chunk = std::max(nsrc, 1);
+                if (mode != MODE_FP64_EXACT) {
+                    int c;
+                    if (chunk_override > 0) {
+                        c = chunk_override;
+                    } else {
+                        // enough CTAs to fill the SMs several times over, but at least
+                        // kMinIter sources per thread in every chunk
+                        const int kMinIter = 48;
+                        const int want = std::max(1, (kTargetCtas + ntile - 1) / ntile);
+                        const int most = std::max(1, nsrc / (kMinIter * lanes));
+                        const int nch = std::max(1, std::min(want, most));
+                        c = (nsrc + nch - 1) / nch;
+                    }
+                    chunk = std::max(c, 1);
+                }
+                const int nchunk = std::max(1, (nsrc + chunk - 1) / chunk);
+                GravItem g;
+                memset(&g, 0, sizeof(g));
+                g.sys = (int)s;
+                g.sink0 = si.off + s0;
+                g.nsink = nsink;
+                g.nchunk = nchunk;
+                g.lanes = lanes;
+                g.cls = q.cls;
+                g.tile = nchunk > 1 ? tiles++ : -1;
+                g.part_off = (int)part;
+                if (nchunk > 1) part += (size_t)nchunk * nsink;
+                for (int c = 0; c < nchunk; c++) {
+                    g.chunk = c;
+                    g.src0 = si.off + q.j0 + c * chunk;
+                    g.src1 = si.off + std::min(q.j1, q.j0 + (c + 1) * chunk);
+                    if (nsrc == 0) g.src0 = g.src1 = si.off;
+                    items.push_back(g);
+                }
+            }
+        }
+}
+}  // namespace redgb
+
 struct red_sim {
     red_config_t cfg;
     int mode = MODE_MIXED;
@@ -416,8 +484,6 @@ void red_sim::build_plan()
     CK(cudaMemcpy(h_radius.data(), radius, n_cap * sizeof(double), cudaMemcpyDeviceToHost));
     size_t part = 0;
     int tiles = 0;
-    const bool fp32 = (mode == MODE_MIXED || mode == MODE_FP32);
-    const int kTargetCtas = 8 * 152;   // ~8 resident CTAs on each of GB300's 152 SMs
     for (uint32_t s = 0; s < n_sys; s++) {
         const SysHost& h = sh[s];
         SysInfo& si = sinfo[s];
@@ -427,61 +493,7 @@ void red_sim::build_plan()
         si.n_SI = (int)h.n_SI();
         si.n_massive = (int)h.n_massive();
         si.n_err = cfg.error_check_for_tp ? si.n : si.n_massive;
-        const int src_start = fp32 ? si.n_star : 0;
-        struct C { int cls, s0, s1, j0, j1; };
-        const C cls[3] = {{CLS_SI, 0, si.n_SI, src_start, si.n_massive},
-                          {CLS_NSI, si.n_SI, si.n_massive, src_start, si.n_SI},
-                          {CLS_NI, si.n_massive, si.n, src_start, si.n_massive}};
-        for (const C& q : cls) {
-            const int nsink_all = q.s1 - q.s0;
-            if (nsink_all <= 0) continue;
-            const int nsrc = std::max(0, q.j1 - q.j0);
-            // threads per sink: a power of two in [4, 32]; few sinks get more lanes
-            int lanes = 4;
-            if (mode != MODE_FP64_EXACT)
-                while (lanes < 32 && lanes < lanes_cap && 2 * lanes * nsink_all <= kTile) lanes *= 2;
-            const int tile_sinks = kTile / lanes;
-            const int ntile = (nsink_all + tile_sinks - 1) / tile_sinks;
-            for (int t = 0; t < ntile; t++) {
-                const int s0 = q.s0 + t * tile_sinks;
-                const int nsink = std::min(tile_sinks, q.s1 - s0);
-                int chunk = std::max(nsrc, 1);
-                if (mode != MODE_FP64_EXACT) {
-                    int c;
-                    if (chunk_override > 0) {
-                        c = chunk_override;
-                    } else {
-                        // enough CTAs to fill the SMs several times over, but at least
-                        // kMinIter sources per thread in every chunk
-                        const int kMinIter = 48;
-                        const int want = std::max(1, (kTargetCtas + ntile - 1) / ntile);
-                        const int most = std::max(1, nsrc / (kMinIter * lanes));
-                        const int nch = std::max(1, std::min(want, most));
-                        c = (nsrc + nch - 1) / nch;
-                    }
-                    chunk = std::max(c, 1);
-                }
-                const int nchunk = std::max(1, (nsrc + chunk - 1) / chunk);
-                GravItem g;
-                memset(&g, 0, sizeof(g));
-                g.sys = (int)s;
-                g.sink0 = si.off + s0;
-                g.nsink = nsink;
-                g.nchunk = nchunk;
-                g.lanes = lanes;
-                g.cls = q.cls;
-                g.tile = nchunk > 1 ? tiles++ : -1;
-                g.part_off = (int)part;
-                if (nchunk > 1) part += (size_t)nchunk * nsink;
-                for (int c = 0; c < nchunk; c++) {
-                    g.chunk = c;
-                    g.src0 = si.off + q.j0 + c * chunk;
-                    g.src1 = si.off + std::min(q.j1, q.j0 + (c + 1) * chunk);
-                    if (nsrc == 0) g.src0 = g.src1 = si.off;
-                    items.push_back(g);
-                }
-            }
-        }
+        plan_gravity_items(si, (int)s, mode, chunk_override, lanes_cap, items, part, tiles);
         for (int b = 0; b < si.n; b += kSegment) segs.push_back(Segment{(int)s, si.off + b, si.off + std::min(si.n, b + kSegment), 0});
         for (int b = 0; b < si.n; b += kFinishBodies)
             fsegs.push_back(Segment{(int)s, si.off + b, si.off + std::min(si.n, b + kFinishBodies), 0});
@@ -1029,6 +1041,8 @@ void red_sim::rebuild_system(uint32_t s)
     catch (const std::bad_alloc&) {                                                                      \
         return set_error(RED_ERR_ARG, "host allocation failed");                                         \
     }
+
+int redgb_set_error(int code, const char* msg) { return set_error(code, "%s", msg); }
 
 static int check_sim(red_sim* sim)
 {

@@ -26,7 +26,7 @@ EXPORTS = ["red_create", "red_destroy", "red_step", "red_launch_tries", "red_syn
            "red_calc_dydx", "red_calc_integral", "red_calc_energy_interacting", "red_get_state",
            "red_set_state", "red_get_system_info", "red_set_dt_next", "red_rebuild_vectors",
            "red_autotune", "red_profile_try", "red_interactions_per_eval", "red_kernel_launches", "red_n_systems",
-           "red_last_error", "red_version"]
+           "red_calc_accel_noalloc", "red_last_error", "red_version"]
 
 
 class RedError(RuntimeError):
@@ -58,6 +58,17 @@ class SystemInfo(C.Structure):
                 ("n_total", C.c_uint32), ("active", C.c_int32), ("halted", C.c_int32), ("status", C.c_int32),
                 ("n_collision", C.c_uint32 * 3), ("n_ejection", C.c_uint32 * 3),
                 ("n_hit_centrum", C.c_uint32 * 3), ("n_event", C.c_uint32 * 3)]
+
+
+class AccelArgs(C.Structure):
+    """red_accel_args_t: device pointers of the allocation-free gravity entry point."""
+    _fields_ = [("playing", C.c_uint32 * 7), ("r", C.c_void_p), ("v", C.c_void_p), ("mass", C.c_void_p),
+                ("radius", C.c_void_p), ("density", C.c_void_p), ("cd", C.c_void_p), ("id", C.c_void_p),
+                ("accel", C.c_void_p), ("precision", C.c_int32), ("gas_disk", C.c_int32), ("gas", GasParams),
+                ("t", C.c_double), ("device", C.c_int32), ("stream", C.c_void_p)]
+
+
+NOALLOC_MAX_BODIES = 32768
 
 
 class Integral(C.Structure):
@@ -101,6 +112,7 @@ def load(path=LIB_PATH):
     L.red_kernel_launches.restype = C.c_uint64
     L.red_n_systems.argtypes = [P]
     L.red_n_systems.restype = C.c_uint32
+    L.red_calc_accel_noalloc.argtypes = [C.POINTER(AccelArgs)]
     L.red_last_error.restype = C.c_char_p
     L.red_version.restype = C.c_char_p
     _lib = L
@@ -114,6 +126,11 @@ def _p(a):
 def _check(rc):
     if rc != RED_OK:
         raise RedError(rc, load().red_last_error().decode())
+
+
+def calc_accel_noalloc(args):
+    """Calls red_calc_accel_noalloc with a filled AccelArgs; raises on error."""
+    _check(load().red_calc_accel_noalloc(C.byref(args)))
 
 
 def gas_struct(gas_record):
