@@ -86,7 +86,8 @@ typedef struct {
     double tolerance;
     int32_t error_check_for_tp;  /* integrator::error_check_for_tp (integrator.h:33) */
     int32_t precision;           /* RED_PREC_* */
-    int32_t stage_exact;         /* 1: stage sums in red's order without FMA (bit-identical); 0: FMA */
+    int32_t stage_exact;         /* stage sums in red's order without FMA (bit-identical): implied by
+                                    RED_PREC_FP64_EXACT, refused (RED_ERR_ARG) with the other modes */
     double threshold[RED_THRESHOLD_N]; /* parameter::threshold (parameter.cpp:214-237) */
     double output_interval;      /* dt_next is clamped to it after every step (main.cu:535-538); 0 = off */
     double length;               /* per-system integration length, code units (main.cu:471); 0 = unbounded */

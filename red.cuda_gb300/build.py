@@ -19,7 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
-UNITS = ["kernels.cu", "sim.cu", "noalloc.cu"]
+UNITS = ["stage_mixed.cu", "stage_fp64.cu", "stage_exact.cu", "stage_fp32.cu", "kernels.cu", "sim.cu", "noalloc.cu"]
 
 
 def nvcc():

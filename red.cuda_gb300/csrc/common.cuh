@@ -1,0 +1,253 @@
+// common.cuh -- device helpers shared by the kernels of libredgb: double-single
+// arithmetic, red's multiply/add order switch, analytic gas drag, the RKF7(8)
+// and RK4 stage combinations, the FP32 position copies.
+#pragma once
+#include <cfloat>
+#include <cstdio>
+
+#include "redgb_dev.cuh"
+
+namespace redgb {
+
+// Integrator tableaux; every translation unit that includes this header has
+// its own copy, loaded by its set_tableau_* function.
+static __constant__ Tableau c_tb;
+
+// Squared softening added to r^2 in the FP32 loops only, so that the self pair
+// (r = 0 exactly) contributes 0 * finite instead of 0 * inf.  For any real pair
+// (r >= 1e-6 AU) it changes the force by < 1e-11 relative, far below FP32
+// rounding.  The FP64 paths use no softening, as red.
+constexpr float kEps2 = 1.0e-24f;
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+
+// Knuth's TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;
+    const float bp = s - a;
+    e = (a - (s - bp)) + (b - bp);
+}
+
+// Folds the FP32 tile sum t into the double-single accumulator (hi, lo).
+__device__ __forceinline__ void ds_add(float& hi, float& lo, float t)
+{
+    float s, e;
+    two_sum(hi, t, s, e);
+    hi = s;
+    lo += e;
+}
+
+// (ah, al) += (bh, bl) for double-single values (TwoSum on the high words,
+// low words added; Dekker 1971 / Knuth TwoSum).
+__device__ __forceinline__ void ds_merge(float& ah, float& al, float bh, float bl)
+{
+    float s, e;
+    two_sum(ah, bh, s, e);
+    ah = s;
+    al = al + bl + e;
+}
+
+__device__ __forceinline__ void split_ds(double x, float& h, float& l)
+{
+    h = __double2float_rn(x);
+    l = __double2float_rn(x - (double)h);
+}
+
+__device__ __forceinline__ void write_pos(float4* hi, float4* lo, int i, double x, double y, double z,
+                                          double m_eff, double radius)
+{
+    float4 H, L;
+    split_ds(x, H.x, L.x);
+    split_ds(y, H.y, L.y);
+    split_ds(z, H.z, L.z);
+    H.w = __double2float_rn(m_eff);
+    L.w = __double2float_rn(radius);
+    hi[i] = H;
+    lo[i] = L;
+}
+
+// Multiply / add that either follows red's -fmad=false arithmetic (EXACT)
+// or lets the compiler fuse.
+template <bool EXACT> __device__ __forceinline__ double mul(double a, double b)
+{
+    return EXACT ? __dmul_rn(a, b) : a * b;
+}
+template <bool EXACT> __device__ __forceinline__ double add(double a, double b)
+{
+    return EXACT ? __dadd_rn(a, b) : a + b;
+}
+template <bool EXACT> __device__ __forceinline__ double sub(double a, double b)
+{
+    return EXACT ? __dsub_rn(a, b) : a - b;
+}
+// a + b * c
+template <bool EXACT> __device__ __forceinline__ double madd(double a, double b, double c)
+{
+    return EXACT ? __dadd_rn(a, __dmul_rn(b, c)) : fma(b, c, a);
+}
+
+// ---------------------------------------------------------------------------
+// analytic gas disk, pp_disk.cu:59-155 and 485-521
+// ---------------------------------------------------------------------------
+static __device__ double gas_reduction_factor(const GasDev& g, double t)
+{
+    switch (g.gas_decrease) {
+    case 0: return 1.0;
+    case 1:
+        if (t <= g.t0) return 1.0;
+        else if (g.t0 < t && t <= g.t1 && g.t0 != g.t1) return 1.0 - (t - g.t0) / (g.t1 - g.t0);
+        else return 0.0;
+    case 2: return exp(-(t - g.t0) / g.e_folding_time);
+    default: return 1.0;
+    }
+}
+
+// Drag factor f and gas velocity (gx, gy, 0) at (r, v): the acceleration is
+// f (v_gas - v) (calc_drag_accel_NSI, pp_disk.cu:485-521).
+static __device__ void drag_factor(const GasDev& g, double decr, double m_star, double rx, double ry, double rz, double vx,
+                            double vy, double vz, double cd, double radius, double density, double& f, double& gx,
+                            double& gy)
+{
+    // gas velocity: circular velocity scaled by sqrt(1 - 2 eta r^p) (pp_disk.cu:107-155)
+    const double r = sqrt(rx * rx + ry * ry);
+    const double vc = sqrt(m_star / r);
+    gx = 0.0;
+    gy = 0.0;
+    if (rx == 0.0 && ry == 0.0) {
+    } else if (ry == 0.0) {
+        gy = rx > 0.0 ? vc : -vc;
+    } else if (rx == 0.0) {
+        gx = ry > 0.0 ? -vc : vc;
+    } else if (rx >= ry) {
+        const double p = ry / rx;
+        gy = rx >= 0 ? vc / sqrt(1.0 + p * p) : -vc / sqrt(1.0 + p * p);
+        gx = -gy * p;
+    } else {
+        const double p = rx / ry;
+        gx = ry >= 0 ? -vc / sqrt(1.0 + p * p) : vc / sqrt(1.0 + p * p);
+        gy = -gx * p;
+    }
+    const double fv = sqrt(1.0 - 2.0 * g.eta[0] * pow(r, g.eta[1]));
+    gx *= fv;
+    gy *= fv;
+    // gas density (pp_disk.cu:86-105)
+    const double h = g.sch[0] * pow(r, g.sch[1]);
+    const double arg = (rz / h) * (rz / h);
+    double dens;
+    if (0.1 < r) {
+        dens = g.rho[0] * pow(r, g.rho[1]) * exp(-arg);
+    } else {
+        const double a = g.rho[0] * pow(0.1, g.rho[1] - 4.0);
+        dens = a * (r * r) * (r * r) * exp(-arg);
+    }
+    const double ux = gx - vx, uy = gy - vy, uz = 0.0 - vz;
+    const double un = sqrt(ux * ux + uy * uy + uz * uz);
+    f = decr * (3.0 * cd * dens * un) / (8.0 * radius * density);
+}
+
+struct alignas(32) D4 {
+    double x, y, z, w;
+};
+
+// Nonzero terms of each RKF7(8) stage row in the order red's stage kernels
+// add them (rk8_kernel::calc_ytemp_for_f1..f12, int_rungekutta8.cu:80-246).
+// Compile-time copies of Tableau::nnz / src so that the combination unrolls.
+__device__ constexpr int kNnz[13] = {0, 1, 2, 2, 3, 3, 4, 4, 6, 7, 8, 6, 9};
+__device__ constexpr int kSrc[13][9] = {
+    {0}, {0}, {0, 1}, {0, 2}, {0, 2, 3}, {0, 3, 4}, {0, 3, 4, 5}, {0, 4, 5, 6},
+    {0, 3, 4, 5, 6, 7}, {0, 3, 4, 5, 6, 7, 8}, {0, 3, 4, 5, 6, 7, 8, 9},
+    {0, 5, 6, 7, 8, 9}, {0, 3, 4, 5, 6, 7, 8, 9, 11}};
+
+// Component x (= 3 i + c) of the ytemp of RKF7(8) stage NX:
+// y + dt * sum_q a_{NX,q} K_q, terms in red's order; loads issued first.
+template <int NX, bool EXACT>
+__device__ __forceinline__ void combine_rkf78(const StageParams& P, double dt, int x, double& out_r, double& out_v)
+{
+    constexpr int nnz = kNnz[NX];
+    constexpr int off = 1 + NX * (NX - 1) / 2;
+    double kr[nnz], kv[nnz];
+#pragma unroll
+    for (int q = 0; q < nnz; q++) {
+        kr[q] = P.Kr[kSrc[NX][q]][x];
+        kv[q] = P.Kv[kSrc[NX][q]][x];
+    }
+    double ar = mul<EXACT>(c_tb.a[off + kSrc[NX][0]], kr[0]);
+    double av = mul<EXACT>(c_tb.a[off + kSrc[NX][0]], kv[0]);
+#pragma unroll
+    for (int q = 1; q < nnz; q++) {
+        const double aq = c_tb.a[off + kSrc[NX][q]];
+        ar = madd<EXACT>(ar, aq, kr[q]);
+        av = madd<EXACT>(av, aq, kv[q]);
+    }
+    out_r = madd<EXACT>(P.y_r[x], dt, ar);
+    out_v = madd<EXACT>(P.y_v[x], dt, av);
+}
+
+// Component x of the ytemp of stage nx (RKF78: y + dt*sum a K in red's term
+// order; RK4: y + (a dt) K, rk4_kernel::sum_vector, int_rungekutta4.cu:36-47).
+template <bool EXACT>
+__device__ __forceinline__ void combine(const StageParams& P, int scheme, int nx, double dt, int x, double& out_r,
+                                        double& out_v)
+{
+    if (scheme == SCHEME_RKF78) {
+        switch (nx) {
+        case 1: combine_rkf78<1, EXACT>(P, dt, x, out_r, out_v); break;
+        case 2: combine_rkf78<2, EXACT>(P, dt, x, out_r, out_v); break;
+        case 3: combine_rkf78<3, EXACT>(P, dt, x, out_r, out_v); break;
+        case 4: combine_rkf78<4, EXACT>(P, dt, x, out_r, out_v); break;
+        case 5: combine_rkf78<5, EXACT>(P, dt, x, out_r, out_v); break;
+        case 6: combine_rkf78<6, EXACT>(P, dt, x, out_r, out_v); break;
+        case 7: combine_rkf78<7, EXACT>(P, dt, x, out_r, out_v); break;
+        case 8: combine_rkf78<8, EXACT>(P, dt, x, out_r, out_v); break;
+        case 9: combine_rkf78<9, EXACT>(P, dt, x, out_r, out_v); break;
+        case 10: combine_rkf78<10, EXACT>(P, dt, x, out_r, out_v); break;
+        case 11: combine_rkf78<11, EXACT>(P, dt, x, out_r, out_v); break;
+        default: combine_rkf78<12, EXACT>(P, dt, x, out_r, out_v); break;
+        }
+    } else {
+        const double bf = mul<EXACT>(c_tb.a4[nx], dt);
+        out_r = madd<EXACT>(P.y_r[x], bf, P.Kr[nx - 1][x]);
+        out_v = madd<EXACT>(P.y_v[x], bf, P.Kv[nx - 1][x]);
+    }
+}
+
+// RK4 y_{n+1} = y + b0 (f1 + f4) + b1 (f2 + f3), b = (1/6, 1/3) * dt
+// (rk4_kernel::calc_y_np1, int_rungekutta4.cu:49-60)
+template <bool EXACT>
+__device__ __forceinline__ double rk4_ynp1(double y, double b0, double b1, double k0, double k1, double k2,
+                                           double k3)
+{
+    return add<EXACT>(madd<EXACT>(y, b0, add<EXACT>(k0, k3)), mul<EXACT>(b1, add<EXACT>(k1, k2)));
+}
+
+// RKF78 y_{n+1} = y + dt (b0 f0 + b5 f5 + b6 (f6 + f7) + b8 (f8 + f9) + b10 f10)
+// (rk8_kernel::calc_y_np1, int_rungekutta8.cu:262-274)
+template <bool EXACT>
+__device__ __forceinline__ double rk8_ynp1(double y, double dt, const double* const* K, int idx)
+{
+    double acc = mul<EXACT>(c_tb.b[0], K[0][idx]);
+    acc = madd<EXACT>(acc, c_tb.b[5], K[5][idx]);
+    acc = madd<EXACT>(acc, c_tb.b[6], add<EXACT>(K[6][idx], K[7][idx]));
+    acc = madd<EXACT>(acc, c_tb.b[8], add<EXACT>(K[8][idx], K[9][idx]));
+    acc = madd<EXACT>(acc, c_tb.b[10], K[10][idx]);
+    return madd<EXACT>(y, dt, acc);
+}
+
+// Writes one component of a stage position: the hi / lo words of coordinate c
+// (c < 3), or the mass of the source and the radius (c == 3).
+__device__ __forceinline__ void write_pos_c(float4* hi, float4* lo, int i, int c, double v)
+{
+    float* H = reinterpret_cast<float*>(hi + i);
+    float* L = reinterpret_cast<float*>(lo + i);
+    if (c < 3) {
+        float h, l;
+        split_ds(v, h, l);
+        H[c] = h;
+        L[c] = l;
+    }
+}
+
+}  // namespace redgb

@@ -176,7 +176,7 @@ extern "C" int red_calc_accel_noalloc(const red_accel_args_t* a)
     P.gas.t1 = a->gas.t1;
     P.gas.e_folding_time = a->gas.e_folding_time;
     P.gas.gas_decrease = a->gas.gas_decrease;
-    launch_stage(P, (int)items.size(), a->precision, a->precision == RED_PREC_FP64_EXACT, st);
+    launch_stage(P, (int)items.size(), a->precision, st);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(RED_ERR_CUDA, cudaGetErrorString(e));
     return RED_OK;

@@ -69,7 +69,10 @@ struct GravItem {
     int part_off;         // first partial record of the tile
     int lanes;            // threads per sink (4, 8, 16 or 32), lanes * nsink <= kTile
     int cls;
-    int pad;
+    int soff;             // first body of the system; its stars are [soff, soff + nstar)
+    int nstar;
+    int nerr;             // bodies [soff, soff + nerr) enter the error norm
+    int pad[3];
 };
 
 // Per-body kernels: one CTA per segment of one system.
@@ -221,9 +224,20 @@ struct EjhcParams {
 void plan_gravity_items(const SysInfo& si, int sys, int mode, int chunk_override, int lanes_cap,
                         std::vector<GravItem>& items, size_t& part, int& tiles);
 
-// Host-side launchers (kernels.cu).
+// Host-side launchers (kernels.cu, stage_*.cu).  The stage kernel's mode
+// fixes the arithmetic of the stage combinations: FP64_EXACT combines in red's
+// operation order without FMA, the other modes with FMA.
 void set_tableau(const Tableau& tb, cudaStream_t s);
-void launch_stage(const StageParams& P, int n_items, int mode, int stage_exact, cudaStream_t s);
+void launch_stage(const StageParams& P, int n_items, int mode, cudaStream_t s);
+int stage_variant(const StageParams& P);
+void set_tableau_mixed(const Tableau& tb, cudaStream_t s);
+void set_tableau_fp32(const Tableau& tb, cudaStream_t s);
+void set_tableau_fp64(const Tableau& tb, cudaStream_t s);
+void set_tableau_exact(const Tableau& tb, cudaStream_t s);
+void launch_stage_mixed(const StageParams& P, int n, int variant, cudaStream_t s);
+void launch_stage_fp32(const StageParams& P, int n, int variant, cudaStream_t s);
+void launch_stage_fp64(const StageParams& P, int n, int variant, cudaStream_t s);
+void launch_stage_exact(const StageParams& P, int n, int variant, cudaStream_t s);
 void launch_prep(const Segment* segs, int n_segs, const SysInfo* sinfo, const DevSys* sys, const double* y_r,
                  const double* mass, const double* radius, const int* id, float4* hi, float4* lo, int all,
                  cudaStream_t s);

@@ -174,7 +174,7 @@ void plan_gravity_items(const SysInfo& si, int s, int mode, int chunk_override, 
                     } else {
                         // enough CTAs to fill the SMs several times over, but at least
                         // kMinIter sources per thread in every chunk
-                        const int kMinIter = 48;
+                        const int kMinIter = 16;
                         const int want = std::max(1, (kTargetCtas + ntile - 1) / ntile);
                         const int most = std::max(1, nsrc / (kMinIter * lanes));
                         const int nch = std::max(1, std::min(want, most));
@@ -191,6 +191,9 @@ void plan_gravity_items(const SysInfo& si, int s, int mode, int chunk_override, 
                 g.nchunk = nchunk;
                 g.lanes = lanes;
                 g.cls = q.cls;
+                g.soff = si.off;
+                g.nstar = si.n_star;
+                g.nerr = si.n_err;
                 g.tile = nchunk > 1 ? tiles++ : -1;
                 g.part_off = (int)part;
                 if (nchunk > 1) part += (size_t)nchunk * nsink;
@@ -369,6 +372,11 @@ void red_sim::create(const red_config_t* c, uint32_t n_systems, const uint32_t* 
     }
     if (cfg.precision < 0 || cfg.precision > 3) throw ArgError{RED_ERR_ARG, "bad precision"};
     mode = cfg.precision;
+    // FP64_EXACT combines the stages in red's order without FMA; the other
+    // modes combine with FMA
+    if (cfg.stage_exact && mode != MODE_FP64_EXACT)
+        throw ArgError{RED_ERR_ARG, "stage_exact requires precision RED_PREC_FP64_EXACT"};
+    if (mode == MODE_FP64_EXACT) cfg.stage_exact = 1;
     device = cfg.device;
     n_sys = n_systems;
     sh.resize(n_sys);
@@ -631,7 +639,7 @@ void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs
     mark(-1);
     for (int s = 0; s < n_stage; s++) {
         StageParams P = stage_params(s, false);
-        launch_stage(P, (int)items.size(), mode, cfg.stage_exact, stream);
+        launch_stage(P, (int)items.size(), mode, stream);
         mark(0);
         n++;
     }
@@ -1237,7 +1245,7 @@ int red_calc_dydx(red_sim* sim, uint32_t sys, int32_t i, double t, red_var4_t* d
         GravItem* d = dalloc<GravItem>(mine.size());
         CK(cudaMemcpy(d, mine.data(), mine.size() * sizeof(GravItem), cudaMemcpyHostToDevice));
         P.items = d;
-        launch_stage(P, (int)mine.size(), sim->mode, sim->cfg.stage_exact, sim->stream);
+        launch_stage(P, (int)mine.size(), sim->mode, sim->stream);
         CK(cudaGetLastError());
         sim->launches++;
         CK(cudaMemcpyAsync(buf.data(), sim->Kv[0] + 3 * (size_t)h.off, buf.size() * sizeof(double),
@@ -1493,10 +1501,10 @@ int red_autotune(red_sim* sim)
         sim->chunk_override = c;
         sim->build_plan();
         StageParams P = sim->stage_params(0, true);
-        for (int w = 0; w < 2; w++) launch_stage(P, (int)sim->items.size(), sim->mode, sim->cfg.stage_exact, sim->stream);
+        for (int w = 0; w < 2; w++) launch_stage(P, (int)sim->items.size(), sim->mode, sim->stream);
         CK(cudaEventRecord(e0, sim->stream));
         const int reps = 5;
-        for (int w = 0; w < reps; w++) launch_stage(P, (int)sim->items.size(), sim->mode, sim->cfg.stage_exact, sim->stream);
+        for (int w = 0; w < reps; w++) launch_stage(P, (int)sim->items.size(), sim->mode, sim->stream);
         CK(cudaEventRecord(e1, sim->stream));
         CK(cudaEventSynchronize(e1));
         sim->launches += 2 + reps;
