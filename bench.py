@@ -43,8 +43,10 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
-def workload(rg, name):
-    """(systems, integrator kwargs, description)."""
+def workload(rg, name, rank=0, world=1):
+    """(systems, integrator kwargs, description) of one rank: the ensemble is
+    split by systems (rank r owns its own 512 seeded disks), a single disk
+    is replicated on every rank."""
     ic = rg.ic
     if name == "c1":
         s = ic.config1()
@@ -57,7 +59,8 @@ def workload(rg, name):
                          collision_factor=1.0), \
             "config3: 1 star + 32 protoplanets + 65503 planetesimals (1-100 km), analytic gas drag, RKF7(8) tol 1e-10"
     if name == "c4":
-        systems = ic.config4()
+        first, count = rg.shard.ensemble_range(512, rank, world)
+        systems = ic.config4(n_systems=count, first=first)
         return systems, dict(integrator="rkf78", adaptive=True, tolerance=1e-10, dt=1.0 * K_GAUSS,
                              collision_factor=1.0), \
             "config4: 512 disks, N ~ U[128, 4096], 2-8 protoplanets each, RKF7(8) tol 1e-10, per-system dt"
@@ -260,7 +263,7 @@ def run_reference(args, rg, rank, world):
 def run_ours(args, rg, rank, world, local_rank):
     import torch
     torch.cuda.set_device(local_rank)
-    systems, kw, desc = workload(rg, args.config)
+    systems, kw, desc = workload(rg, args.config, rank, world)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -280,12 +283,12 @@ def run_ours(args, rg, rank, world, local_rank):
     tried_before = sum(sim.info(k).n_tried for k in range(sim.n_systems))
     launches0 = sim.kernel_launches
     clocks = ClockSampler(local_rank)
-    if world > 1:
-        torch.distributed.barrier()
+    rg.shard.barrier(local_rank)
     torch.cuda.synchronize()
     clocks.start()
     ms = timed_steps(torch, sim, stream, args.steps, flush)
     torch.cuda.synchronize()
+    rg.shard.barrier(local_rank)
     clk = clocks.stop()
     launches = sim.kernel_launches - launches0
     drain_events(sim)
@@ -296,11 +299,7 @@ def run_ours(args, rg, rank, world, local_rank):
     E1 = sim.energy_interacting(0)
     dE = abs((E1[0] - E0[0]) / E0[0])
     inter = ipe * ns * args.steps
-    t_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
+    t_max = rg.shard.max_over_ranks(ms, device="cuda")
     value = inter * world / (t_max * 1e-3)
     sim_years = sim_dt / K_GAUSS / YEAR
     # roofline of the dominant kernel (kernel-by-kernel tries, CUDA events)
@@ -319,21 +318,22 @@ def run_ours(args, rg, rank, world, local_rank):
     st = sim.get_state(0)
     host = {f: torch.from_numpy(getattr(st, f).view(np.uint8)).pin_memory() for f in ("r", "v", "p", "md")}
     e2e_steps = max(3, args.steps // 2)
+    st.r = host["r"].numpy().view(rg.types.VAR4)
+    st.v = host["v"].numpy().view(rg.types.VAR4)
+    st.p = host["p"].numpy().view(rg.types.PARAM)
+    st.md = host["md"].numpy().view(rg.types.BMD)
     torch.cuda.synchronize()
+    rg.shard.barrier(local_rank)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        st.r = host["r"].numpy().view(rg.types.VAR4)
-        st.v = host["v"].numpy().view(rg.types.VAR4)
-        sim.set_state(0, st)
+        sim.set_state(0, st, parts="rv")      # inputs from pinned host memory
         sim.step()
-        out = sim.get_state(0)
-        host["r"].numpy()[:] = out.r.view(np.uint8)
-        host["v"].numpy()[:] = out.v.view(np.uint8)
-    e2e_s = time.perf_counter() - t0
+        sim.get_state(0, out=st, parts="rv")  # results into the same pinned buffers
+    e2e_s = rg.shard.max_over_ranks(time.perf_counter() - t0, device="cuda")
     drain_events(sim)
     tried_e2e = sim.info(0).n_tried
     e2e_value = ipe * ns * e2e_steps * world / e2e_s
-    bytes_state = n0 * (32 + 32 + 32 + 24)
+    bytes_state = n0 * (32 + 32)
 
     # the plain FP64 path on the same GPU, same workload (fewer steps)
     fp64 = None
@@ -365,7 +365,7 @@ def run_ours(args, rg, rank, world, local_rank):
                 "tries_in_timed_region": int(tried), "accept_fraction": None,
                 "e2e": {"value": e2e_value, "unit": "interactions/s", "h2d_bytes_per_step": bytes_state,
                         "d2h_bytes_per_step": bytes_state, "steps": e2e_steps,
-                        "api": "red_set_state + red_step + red_get_state"},
+                        "api": "red_set_state(r, v) + red_step + red_get_state(r, v)"},
                 "roofline": roof,
                 "cpu_baseline": cpu,
                 "plain_fp64_same_gpu": fp64,

@@ -347,6 +347,51 @@ __global__ void __launch_bounds__(kSegment) k_potential(const Segment* segs, con
 }
 
 // ---------------------------------------------------------------------------
+// host transfers: one system's bodies between the device's structure of
+// arrays and the caller's records (var4_t r, v; param_t p; id and body type),
+// packed as rvp = [r: 4n | v: 4n | p: 4n] doubles and ib = [id, type] x n
+// ---------------------------------------------------------------------------
+__global__ void k_pack_state(int o, int n, const double* y_r, const double* y_v, const double* mass,
+                             const double* radius, const double* density, const double* cd, const int* id,
+                             const int* btype, double* rvp, int* ib)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) {
+        ib[2 * k] = id[o + k];
+        ib[2 * k + 1] = btype[o + k];
+    }
+    if (k >= 12LL * n) return;
+    const int seg = (int)(k / (4LL * n));
+    const int w = (int)(k - seg * 4LL * n);
+    const int i = o + w / 4, c = w % 4;
+    double v;
+    if (seg == 0) v = c < 3 ? y_r[3 * i + c] : 0.0;
+    else if (seg == 1) v = c < 3 ? y_v[3 * i + c] : 0.0;
+    else v = c == 0 ? mass[i] : (c == 1 ? radius[i] : (c == 2 ? density[i] : cd[i]));
+    rvp[k] = v;
+}
+
+// Inverse of k_pack_state for the parts named in `what` (1 r, 2 v, 4 p, 8 id).
+__global__ void k_unpack_state(int o, int n, int what, const double* rvp, const int* ib, double* y_r, double* y_v,
+                               double* mass, double* radius, double* density, double* cd, int* id)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n && (what & 8)) id[o + k] = ib[2 * k];
+    if (k >= 12LL * n) return;
+    const int seg = (int)(k / (4LL * n));
+    if (!(what & (1 << seg))) return;
+    const int w = (int)(k - seg * 4LL * n);
+    const int i = o + w / 4, c = w % 4;
+    const double v = rvp[k];
+    if (seg == 0) { if (c < 3) y_r[3 * i + c] = v; }
+    else if (seg == 1) { if (c < 3) y_v[3 * i + c] = v; }
+    else if (c == 0) mass[i] = v;
+    else if (c == 1) radius[i] = v;
+    else if (c == 2) density[i] = v;
+    else cd[i] = v;
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 void set_tableau(const Tableau& tb, cudaStream_t s)
@@ -408,6 +453,25 @@ void launch_collision(const CollParams& P, int n_items, int n_segs, bool use_gri
         k_grid_insert<<<n_segs, kSegment, 0, s>>>(P);
         k_grid_query<<<n_segs, kSegment, 0, s>>>(P);
     }
+}
+
+void launch_pack_state(int o, int n, const double* y_r, const double* y_v, const double* mass, const double* radius,
+                       const double* density, const double* cd, const int* id, const int* btype, double* rvp,
+                       int* ib, cudaStream_t s)
+{
+    if (n <= 0) return;
+    const long long tot = 12LL * n;
+    k_pack_state<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(o, n, y_r, y_v, mass, radius, density, cd, id, btype,
+                                                               rvp, ib);
+}
+
+void launch_unpack_state(int o, int n, int what, const double* rvp, const int* ib, double* y_r, double* y_v,
+                         double* mass, double* radius, double* density, double* cd, int* id, cudaStream_t s)
+{
+    if (n <= 0) return;
+    const long long tot = 12LL * n;
+    k_unpack_state<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(o, n, what, rvp, ib, y_r, y_v, mass, radius,
+                                                                 density, cd, id);
 }
 
 void launch_ejhc(const EjhcParams& P, int n_segs, cudaStream_t s)

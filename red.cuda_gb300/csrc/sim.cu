@@ -146,66 +146,80 @@ namespace redgb {
 void plan_gravity_items(const SysInfo& si, int s, int mode, int chunk_override, int lanes_cap,
                         std::vector<GravItem>& items, size_t& part, int& tiles)
 {
-    const int kTargetCtas = 8 * 152;   // ~8 resident CTAs on each of GB300's 152 SMs
+    // enough CTAs for several waves of ~6 resident CTAs on each of GB300's 152 SMs
+    const int kTargetCtas = 8 * 6 * 152;
     const bool fp32 = (mode == MODE_MIXED || mode == MODE_FP32);
-        const int src_start = fp32 ? si.n_star : 0;
-        struct C { int cls, s0, s1, j0, j1; };
-        const C cls[3] = {{CLS_SI, 0, si.n_SI, src_start, si.n_massive},
-                          {CLS_NSI, si.n_SI, si.n_massive, src_start, si.n_SI},
-                          {CLS_NI, si.n_massive, si.n, src_start, si.n_massive}};
-        for (const C& q : cls) {
-            const int nsink_all = q.s1 - q.s0;
-            if (nsink_all <= 0) continue;
-            const int nsrc = std::max(0, q.j1 - q.j0);
-            // threads per sink: a power of two in [4, 32]; few sinks get more lanes
-            int lanes = 4;
-            if (mode != MODE_FP64_EXACT)
-                while (lanes < 32 && lanes < lanes_cap && 2 * lanes * nsink_all <= kTile) lanes *= 2;
-            const int tile_sinks = kTile / lanes;
-            const int ntile = (nsink_all + tile_sinks - 1) / tile_sinks;
-            for (int t = 0; t < ntile; t++) {
-                const int s0 = q.s0 + t * tile_sinks;
-                const int nsink = std::min(tile_sinks, q.s1 - s0);
-                int chunk = std::max(nsrc, 1);
-                if (mode != MODE_FP64_EXACT) {
-                    int c;
-                    if (chunk_override > 0) {
-                        c = chunk_override;
-                    } else {
-                        // enough CTAs to fill the SMs several times over, but at least
-                        // kMinIter sources per thread in every chunk
-                        const int kMinIter = 16;
-                        const int want = std::max(1, (kTargetCtas + ntile - 1) / ntile);
-                        const int most = std::max(1, nsrc / (kMinIter * lanes));
-                        const int nch = std::max(1, std::min(want, most));
-                        c = (nsrc + nch - 1) / nch;
-                    }
-                    chunk = std::max(c, 1);
-                }
-                const int nchunk = std::max(1, (nsrc + chunk - 1) / chunk);
-                GravItem g;
-                memset(&g, 0, sizeof(g));
-                g.sys = (int)s;
-                g.sink0 = si.off + s0;
-                g.nsink = nsink;
-                g.nchunk = nchunk;
-                g.lanes = lanes;
-                g.cls = q.cls;
-                g.soff = si.off;
-                g.nstar = si.n_star;
-                g.nerr = si.n_err;
-                g.tile = nchunk > 1 ? tiles++ : -1;
-                g.part_off = (int)part;
-                if (nchunk > 1) part += (size_t)nchunk * nsink;
-                for (int c = 0; c < nchunk; c++) {
-                    g.chunk = c;
-                    g.src0 = si.off + q.j0 + c * chunk;
-                    g.src1 = si.off + std::min(q.j1, q.j0 + (c + 1) * chunk);
-                    if (nsrc == 0) g.src0 = g.src1 = si.off;
-                    items.push_back(g);
-                }
+    const int src_start = fp32 ? si.n_star : 0;
+    struct C { int cls, s0, s1, j0, j1; };
+    const C cls[3] = {{CLS_SI, 0, si.n_SI, src_start, si.n_massive},
+                      {CLS_NSI, si.n_SI, si.n_massive, src_start, si.n_SI},
+                      {CLS_NI, si.n_massive, si.n, src_start, si.n_massive}};
+    for (const C& q : cls) {
+        const int nsink_all = q.s1 - q.s0;
+        if (nsink_all <= 0) continue;
+        const int nsrc = std::max(0, q.j1 - q.j0);
+        // threads per sink group: a power of two in [4, 32].  Many sinks in the FP32
+        // modes: 8 lanes serving 2 sinks each (each source read feeds two
+        // interactions).  Few sinks: more lanes, the more the longer the source list.
+        int lanes = 4, spt = 1;
+        if (mode != MODE_FP64_EXACT) {
+            if (fp32 && nsink_all >= 32 && lanes_cap >= 8) {
+                lanes = 8;
+                spt = 2;
+            } else {
+                while (lanes < 32 && lanes < lanes_cap &&
+                       (2 * lanes * nsink_all <= kTile || 256 * 2 * lanes <= nsrc))
+                    lanes *= 2;
             }
         }
+        const int tile_sinks = kTile / lanes * spt;
+        const int ntile = (nsink_all + tile_sinks - 1) / tile_sinks;
+        for (int t = 0; t < ntile; t++) {
+            const int s0 = q.s0 + t * tile_sinks;
+            const int nsink = std::min(tile_sinks, q.s1 - s0);
+            int chunk = std::max(nsrc, 1);
+            if (mode != MODE_FP64_EXACT) {
+                int c;
+                if (chunk_override > 0) {
+                    c = chunk_override;
+                } else {
+                    // enough CTAs to fill the SMs several times over, but at least
+                    // kMinIter sources per thread in every chunk; chunks longer than a
+                    // tile are whole tiles
+                    const int kMinIter = 16;
+                    const int want = std::max(1, (kTargetCtas + ntile - 1) / ntile);
+                    const int most = std::max(1, nsrc / (kMinIter * lanes));
+                    const int nch = std::max(1, std::min(want, most));
+                    c = (nsrc + nch - 1) / nch;
+                    if (c > kTile) c = (c + kTile - 1) / kTile * kTile;
+                }
+                chunk = std::max(c, 1);
+            }
+            const int nchunk = std::max(1, (nsrc + chunk - 1) / chunk);
+            GravItem g;
+            memset(&g, 0, sizeof(g));
+            g.sys = (int)s;
+            g.sink0 = si.off + s0;
+            g.nsink = nsink;
+            g.nchunk = nchunk;
+            g.lanes = lanes;
+            g.spt = spt;
+            g.cls = q.cls;
+            g.soff = si.off;
+            g.nstar = si.n_star;
+            g.nerr = si.n_err;
+            g.tile = nchunk > 1 ? tiles++ : -1;
+            g.part_off = (int)part;
+            if (nchunk > 1) part += (size_t)nchunk * nsink;
+            for (int c = 0; c < nchunk; c++) {
+                g.chunk = c;
+                g.src0 = si.off + q.j0 + c * chunk;
+                g.src1 = si.off + std::min(q.j1, q.j0 + (c + 1) * chunk);
+                if (nsrc == 0) g.src0 = g.src1 = si.off;
+                items.push_back(g);
+            }
+        }
+    }
 }
 }  // namespace redgb
 
@@ -257,6 +271,13 @@ struct red_sim {
     unsigned int* d_nev = nullptr;
     uint32_t ev_cap = 0;
     double* d_u = nullptr;
+    // host transfers: device records (k_pack_state layout) and a pinned host copy
+    char* d_xfer = nullptr;
+    char* h_xfer = nullptr;
+    size_t xfer_cap = 0;
+    void ensure_xfer(size_t bytes);
+    void pack_to_host(uint32_t s);
+    std::vector<double> grid_rmax;   // largest small-body radius the collision grid was planned for
 
     // plan
     std::vector<GravItem> items;
@@ -338,6 +359,8 @@ red_sim::~red_sim()
     cudaFree(partial); cudaFree(tile_cnt); cudaFree(d_sys); cudaFree(d_sinfo); cudaFree(d_items);
     cudaFree(d_segs); cudaFree(d_pairs); cudaFree(d_events); cudaFree(d_nev); cudaFree(d_u);
     cudaFree(d_grid); cudaFree(d_head); cudaFree(d_next); cudaFree(d_cell); cudaFree(d_fsegs);
+    cudaFree(d_xfer);
+    if (h_xfer) cudaFreeHost(h_xfer);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -486,6 +509,7 @@ void red_sim::build_plan()
     pairs.clear();
     sinfo.assign(n_sys, SysInfo{});
     grid.assign(n_sys, GridInfo{});
+    grid_rmax.assign(n_sys, 0.0);
     size_t table = 0;
     // radii, for the cell size of the collision grid
     std::vector<double> h_radius(n_cap);
@@ -517,6 +541,7 @@ void red_sim::build_plan()
         const int n_small = si.n - si.n_SI;
         double rmax = 0.0;
         for (int k = si.n_SI; k < si.n; k++) rmax = std::max(rmax, h_radius[si.off + k]);
+        grid_rmax[s] = rmax;
         const double factor = cfg.threshold[RED_THRESHOLD_RADII_ENHANCE_FACTOR];
         if (n_small > 1 && rmax > 0.0 && factor > 0.0) {
             // cell edge >= the largest collision distance f (R_i + R_j) of two small
@@ -1350,20 +1375,59 @@ int red_calc_energy_interacting(red_sim* sim, uint32_t sys, double out[4])
     GUARD_END
 }
 
+// Bytes of the transfer records of n bodies: r, v, p as 12 doubles, id and type as 2 ints.
+static size_t xfer_bytes(size_t n) { return n * (12 * sizeof(double) + 2 * sizeof(int)); }
+
+void red_sim::ensure_xfer(size_t bytes)
+{
+    if (bytes <= xfer_cap) return;
+    cudaFree(d_xfer);
+    if (h_xfer) cudaFreeHost(h_xfer);
+    d_xfer = nullptr;
+    h_xfer = nullptr;
+    xfer_cap = 0;
+    CK(cudaMalloc(&d_xfer, bytes));
+    CK(cudaMallocHost(&h_xfer, bytes));
+    xfer_cap = bytes;
+}
+
+// System s's records, packed on the device and copied into h_xfer in one transfer.
+void red_sim::pack_to_host(uint32_t s)
+{
+    const SysHost& h = sh[s];
+    const size_t n = h.n;
+    ensure_xfer(xfer_bytes(n));
+    double* rvp = (double*)d_xfer;
+    int* ib = (int*)(d_xfer + 12 * n * sizeof(double));
+    launch_pack_state((int)h.off, (int)n, y_r, y_v, mass, radius, density, cd, id, btype, rvp, ib, stream);
+    CK(cudaGetLastError());
+    launches++;
+    CK(cudaMemcpyAsync(h_xfer, d_xfer, xfer_bytes(n), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+}
+
 int red_get_state(red_sim* sim, uint32_t sys, red_var4_t* r, red_var4_t* v, red_param_t* p,
                   red_body_metadata_t* md)
 {
     if (int rc = check_sim(sim)) return rc;
     if (sys >= sim->n_sys) return set_error(RED_ERR_ARG, "bad system index");
     GUARD_BEGIN
-    CK(cudaStreamSynchronize(sim->stream));
-    HostState hs;
-    sim->get_host_state(sys, hs);
-    const size_t n = hs.r.size();
-    if (r) memcpy(r, hs.r.data(), n * sizeof(red_var4_t));
-    if (v) memcpy(v, hs.v.data(), n * sizeof(red_var4_t));
-    if (p) memcpy(p, hs.p.data(), n * sizeof(red_param_t));
-    if (md) memcpy(md, hs.md.data(), n * sizeof(red_body_metadata_t));
+    sim->pack_to_host(sys);
+    const SysHost& h = sim->sh[sys];
+    const size_t n = h.n;
+    const double* rvp = (const double*)sim->h_xfer;
+    const int* ib = (const int*)(sim->h_xfer + 12 * n * sizeof(double));
+    if (r) memcpy(r, rvp, n * sizeof(red_var4_t));
+    if (v) memcpy(v, rvp + 4 * n, n * sizeof(red_var4_t));
+    if (p) memcpy(p, rvp + 8 * n, n * sizeof(red_param_t));
+    if (md) {
+        for (size_t i = 0; i < n; i++) {
+            md[i].id = ib[2 * i];
+            md[i].body_type = ib[2 * i + 1];
+            md[i].mig_type = sim->mig_type[h.off + i];
+            md[i].mig_stop_at = sim->mig_stop_at[h.off + i];
+        }
+    }
     return RED_OK;
     GUARD_END
 }
@@ -1374,20 +1438,49 @@ int red_set_state(red_sim* sim, uint32_t sys, const red_var4_t* r, const red_var
     if (int rc = check_sim(sim)) return rc;
     if (sys >= sim->n_sys) return set_error(RED_ERR_ARG, "bad system index");
     GUARD_BEGIN
-    CK(cudaStreamSynchronize(sim->stream));
-    HostState hs;
-    sim->get_host_state(sys, hs);
-    const size_t n = hs.r.size();
-    if (r) memcpy(hs.r.data(), r, n * sizeof(red_var4_t));
-    if (v) memcpy(hs.v.data(), v, n * sizeof(red_var4_t));
-    if (p) memcpy(hs.p.data(), p, n * sizeof(red_param_t));
+    const SysHost& h = sim->sh[sys];
+    const size_t n = h.n;
+    sim->ensure_xfer(xfer_bytes(n));
+    double* rvp = (double*)sim->h_xfer;
+    int* ib = (int*)(sim->h_xfer + 12 * n * sizeof(double));
     if (md) {
+        // body types are fixed by the class ranges: read the current ones first
+        sim->pack_to_host(sys);
         for (size_t i = 0; i < n; i++)
-            if (md[i].body_type != hs.md[i].body_type)
+            if (md[i].body_type != ib[2 * i + 1])
                 return set_error(RED_ERR_ARG, "body types cannot change through red_set_state");
-        memcpy(hs.md.data(), md, n * sizeof(red_body_metadata_t));
+    } else {
+        CK(cudaStreamSynchronize(sim->stream));   // h_xfer may still feed a transfer
     }
-    sim->put_host_state(sys, hs);
+    int what = 0;
+    if (r) { memcpy(rvp, r, n * sizeof(red_var4_t)); what |= 1; }
+    if (v) { memcpy(rvp + 4 * n, v, n * sizeof(red_var4_t)); what |= 2; }
+    if (p) { memcpy(rvp + 8 * n, p, n * sizeof(red_param_t)); what |= 4; }
+    if (md) {
+        for (size_t i = 0; i < n; i++) {
+            ib[2 * i] = md[i].id;
+            sim->mig_type[h.off + i] = md[i].mig_type;
+            sim->mig_stop_at[h.off + i] = md[i].mig_stop_at;
+        }
+        what |= 8;
+    }
+    CK(cudaMemcpyAsync(sim->d_xfer, sim->h_xfer, xfer_bytes(n), cudaMemcpyHostToDevice, sim->stream));
+    launch_unpack_state((int)h.off, (int)n, what, (const double*)sim->d_xfer,
+                        (const int*)(sim->d_xfer + 12 * n * sizeof(double)), sim->y_r, sim->y_v, sim->mass,
+                        sim->radius, sim->density, sim->cd, sim->id, sim->stream);
+    CK(cudaGetLastError());
+    sim->launches++;
+    bool replan = false;
+    if (p) {
+        // the collision grid's cells must stay wider than the largest collision distance
+        double rmax = 0.0;
+        for (size_t k = h.n_SI(); k < n; k++) rmax = std::max(rmax, p[k].radius);
+        replan = rmax > sim->grid_rmax[sys];
+    }
+    if (replan) {
+        CK(cudaStreamSynchronize(sim->stream));
+        sim->build_plan();
+    }
     sim->prep_positions();
     CK(cudaStreamSynchronize(sim->stream));
     return RED_OK;

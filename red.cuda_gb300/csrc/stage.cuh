@@ -79,28 +79,237 @@ __device__ __forceinline__ double sum_records(const double* base, long long stri
     return a;
 }
 
+
+// 8-byte asynchronous copy global -> shared (cp.async, no register held while
+// the copy is in flight), its commit and the wait for all of a thread's copies.
+__device__ __forceinline__ void cp_async8(void* dst, const void* src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Operands of the epilogue of variant V, staged in shared memory by cp.async
+// at the start of the kernel: slot [slot][t] belongs to element thread t.
+constexpr int kMaxElem = 96;   // 3 * 32 sinks: the largest tile the planner makes
+__host__ __device__ constexpr int var_nk(int v)
+{
+    return v == 1 ? 1 : v == 2 ? 2 : v == 3 ? 2 : v == 4 ? 3 : v == 5 ? 3 : v == 6 ? 4 : v == 7 ? 4 : v == 8 ? 6
+         : v == 9 ? 7 : v == 10 ? 8 : v == 11 ? 6 : v == 12 ? 9 : (v == 14 || v == 15) ? 3 : v == 16 ? 1 : 0;
+}
+template <int V> struct Ops {
+    static constexpr int nk = var_nk(V);
+    static constexpr int VS = 0, YR = 1, YV = 2, M = 3, RAD = 4, KR = 5, KV = 5 + nk, N = 5 + 2 * nk;
+};
+// Stage index of operand q of variant V.
+template <int V> __device__ __forceinline__ int op_src(int q)
+{
+    if constexpr (V >= 1 && V <= 12) return kSrc[V][q];
+    else if constexpr (V == 14) return q;
+    else if constexpr (V == 15) return q == 0 ? 0 : (q == 1 ? 10 : 11);
+    else return 3;
+}
+
+// Gravity of the chunk's sources on SPT sinks per thread, FP32 modes.  The
+// first tile is in shared memory; (th, tl) carry the prefetch of the next.
+// On return thread lane l < 3 SPT of its sink group holds component l % 3 of
+// sink slot (group * SPT + l / 3) in `mine`.
+template <int MODE, int SPT>
+__device__ __forceinline__ void gravity_f32(SmemStage& sm, const StageParams& P, const GravItem& it, float4& th,
+                                            float4& tl, double& mine, int& mine_k, bool& mine_ok)
+{
+    const int t = threadIdx.x;
+    const int L = it.lanes;
+    const int grp = t / L, lane = t % L;
+    float4 H[SPT], Lo[SPT];
+#pragma unroll
+    for (int q = 0; q < SPT; q++) {
+        const int k = grp * SPT + q;
+        const int i = it.sink0 + (k < it.nsink ? k : 0);   // inactive slots shadow sink 0 (results unused)
+        H[q] = P.pos_hi_in[i];
+        Lo[q] = MODE == MODE_MIXED ? P.pos_lo_in[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    float acc[SPT][6];
+#pragma unroll
+    for (int q = 0; q < SPT; q++)
+#pragma unroll
+        for (int c = 0; c < 6; c++) acc[q][c] = 0.f;
+    for (int j0 = it.src0; j0 < it.src1; j0 += kTile) {
+        const int nj = min(kTile, it.src1 - j0);
+        const bool more = j0 + kTile < it.src1;
+        if (more && t < min(kTile, it.src1 - j0 - kTile)) {
+            th = P.pos_hi_in[j0 + kTile + t];
+            if (MODE == MODE_MIXED) tl = P.pos_lo_in[j0 + kTile + t];
+        }
+        float tx[SPT], ty[SPT], tz[SPT];
+#pragma unroll
+        for (int q = 0; q < SPT; q++) tx[q] = ty[q] = tz[q] = 0.f;
+#pragma unroll 4
+        for (int jj = lane; jj < nj; jj += L) {
+            const float4 h = sm.src.f.hi[jj];
+            float4 l = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (MODE == MODE_MIXED) l = sm.src.f.lo[jj];
+#pragma unroll
+            for (int q = 0; q < SPT; q++) {
+                float dx, dy, dz;
+                if (MODE == MODE_MIXED) {
+                    dx = (h.x - H[q].x) + (l.x - Lo[q].x);
+                    dy = (h.y - H[q].y) + (l.y - Lo[q].y);
+                    dz = (h.z - H[q].z) + (l.z - Lo[q].z);
+                } else {
+                    dx = h.x - H[q].x;
+                    dy = h.y - H[q].y;
+                    dz = h.z - H[q].z;
+                }
+                const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, kEps2)));
+                const float ri = rsqrtf(r2);
+                const float ri2 = ri * ri;
+                const float sc = h.w * ri * ri2;
+                tx[q] = fmaf(sc, dx, tx[q]);
+                ty[q] = fmaf(sc, dy, ty[q]);
+                tz[q] = fmaf(sc, dz, tz[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < SPT; q++) {
+            ds_add(acc[q][0], acc[q][1], tx[q]);
+            ds_add(acc[q][2], acc[q][3], ty[q]);
+            ds_add(acc[q][4], acc[q][5], tz[q]);
+        }
+        if (more) {
+            __syncthreads();
+            sm.src.f.hi[t] = th;
+            if (MODE == MODE_MIXED) sm.src.f.lo[t] = tl;
+            __syncthreads();
+        }
+    }
+    // lanes -> one double-single sum per (sink, component): TwoSum in FP32 over a
+    // fixed butterfly, so every lane of the group ends with the same bits
+    for (int o = 1; o < L; o <<= 1) {
+#pragma unroll
+        for (int q = 0; q < SPT; q++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const float oh = __shfl_xor_sync(0xffffffffu, acc[q][2 * c], o);
+                const float ol = __shfl_xor_sync(0xffffffffu, acc[q][2 * c + 1], o);
+                ds_merge(acc[q][2 * c], acc[q][2 * c + 1], oh, ol);
+            }
+    }
+    float hh = 0.f, ll = 0.f;
+#pragma unroll
+    for (int q = 0; q < SPT; q++)
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            if (lane == 3 * q + c) {
+                hh = acc[q][2 * c];
+                ll = acc[q][2 * c + 1];
+            }
+    mine = (double)hh + (double)ll;
+    mine_k = grp * SPT + lane / 3;
+    mine_ok = lane < 3 * SPT && mine_k < it.nsink;
+}
+
+// Gravity of the chunk's sources, FP64 modes (one sink per thread group).
+template <int MODE>
+__device__ __forceinline__ void gravity_f64(SmemStage& sm, const StageParams& P, const GravItem& it, D4& td, int& tid,
+                                            double& mine, int& mine_k, bool& mine_ok)
+{
+    const int t = threadIdx.x;
+    const int L = it.lanes;
+    const int k = t / L, lane = t % L;
+    const bool has = k < it.nsink;
+    const int i = it.sink0 + (has ? k : 0);
+    const double xi = P.r_in[3 * i], yi = P.r_in[3 * i + 1], zi = P.r_in[3 * i + 2];
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int j0 = it.src0; j0 < it.src1; j0 += kTile) {
+        const int nj = min(kTile, it.src1 - j0);
+        const bool more = j0 + kTile < it.src1;
+        if (more && t < min(kTile, it.src1 - j0 - kTile)) {
+            const int j = j0 + kTile + t;
+            tid = P.id[j];
+            const double m = P.mass[j];
+            td = D4{P.r_in[3 * j], P.r_in[3 * j + 1], P.r_in[3 * j + 2], (MODE == MODE_FP64 && tid < 0) ? 0.0 : m};
+        }
+        if (has) {
+            if (MODE == MODE_FP64_EXACT) {
+                // calc_grav_accel_naive, pp_disk.cu:389-413, bit for bit: lane 0 alone,
+                // sources in index order
+                if (lane == 0) {
+                    for (int jj = 0; jj < nj; jj++) {
+                        const D4 q = sm.src.d.d[jj];
+                        if (j0 + jj == i || 0 > sm.src.d.id[jj]) continue;
+                        const double dx = __dsub_rn(q.x, xi), dy = __dsub_rn(q.y, yi), dz = __dsub_rn(q.z, zi);
+                        double w = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+                        const double d = __dsqrt_rn(w);
+                        w = __ddiv_rn(q.w, __dmul_rn(d, w));
+                        ax = __dadd_rn(ax, __dmul_rn(w, dx));
+                        ay = __dadd_rn(ay, __dmul_rn(w, dy));
+                        az = __dadd_rn(az, __dmul_rn(w, dz));
+                    }
+                }
+            } else {
+                for (int jj = lane; jj < nj; jj += L) {
+                    const D4 q = sm.src.d.d[jj];
+                    const double dx = q.x - xi, dy = q.y - yi, dz = q.z - zi;
+                    const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+                    double ri = rsqrt(r2);
+                    ri = r2 > 0.0 ? ri : 0.0;
+                    const double sc = q.w * ri * ri * ri;
+                    ax = fma(sc, dx, ax);
+                    ay = fma(sc, dy, ay);
+                    az = fma(sc, dz, az);
+                }
+            }
+        }
+        if (more) {
+            __syncthreads();
+            sm.src.d.d[t] = td;
+            sm.src.d.id[t] = tid;
+            __syncthreads();
+        }
+    }
+    if (MODE == MODE_FP64_EXACT) {
+        const int gbase = (t & 31) & ~(L - 1);
+        ax = __shfl_sync(0xffffffffu, ax, gbase);
+        ay = __shfl_sync(0xffffffffu, ay, gbase);
+        az = __shfl_sync(0xffffffffu, az, gbase);
+    } else {
+        ax = group_sum(ax, L);
+        ay = group_sum(ay, L);
+        az = group_sum(az, L);
+    }
+    mine = lane == 0 ? ax : (lane == 1 ? ay : az);
+    mine_k = k;
+    mine_ok = has && lane < 3;
+}
+
 // ---------------------------------------------------------------------------
 // k_stage
 //
-// Thread layout of the gravity loop: each sink is served by `lanes`
-// consecutive threads of one warp (lanes in {4, 8, 16, 32}); the lanes split
-// the sources of every shared-memory tile and combine their partial sums with
-// a butterfly of shuffles (every lane ends with the same bits).  The epilogue
-// is element-wise: thread t < 3 nsink owns component x = 3 sink0 + t, which is
-// contiguous in HBM, so every FP64 instruction runs in full warps.
+// Gravity: each group of `lanes` consecutive threads of a warp serves SPT
+// sinks (SPT = 2 in the FP32 modes when the class has many sinks, so that
+// every source read from shared memory feeds two interactions); the lanes
+// split the sources of every tile.  Epilogue: element-wise, thread t < 3 nsink
+// owns component x = 3 sink0 + t, which is contiguous in HBM, so every FP64
+// instruction runs in full warps.
 //
 // Memory round trips on the critical path: the work item; then, in one batch,
-// the system state, the first source tile, the sink's operands for the
-// epilogue and the star / drag inputs; then one trip per further source tile
-// (prefetched into registers while the previous tile is in use); then, for a
-// chunked tile, the partial records of the reduction.
+// the system state, the first source tile, the sinks and the star / drag
+// inputs; then one per further source tile (fetched while the previous one is
+// in use); then, for a chunked tile, the partial records.  The epilogue's
+// operands (y, the K vectors of the combination) are copied into shared
+// memory by cp.async at the start, so they arrive during the gravity loop
+// without holding registers.
 // ---------------------------------------------------------------------------
 template <int MODE, bool EXACT, int V>
-__global__ void __launch_bounds__(kTile) k_stage(const StageParams P)
+__global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
 {
     constexpr bool kF32 = (MODE == MODE_MIXED || MODE == MODE_FP32);
     constexpr bool kRkf = (V >= 1 && V <= 12);
+    using O = Ops<V>;
     __shared__ SmemStage sm;
+    __shared__ double ops[O::N][kMaxElem];
     const GravItem it = P.items[blockIdx.x];
     const int s = P.stage;
     DevSys* S = P.sys + it.sys;
@@ -111,58 +320,25 @@ __global__ void __launch_bounds__(kTile) k_stage(const StageParams P)
         dt = S->dt_try;
         if (!(act && !hal && quo != 0)) return;   // uniform over the CTA
     }
-
-    const int L = it.lanes;
     const int t = threadIdx.x;
-    const int k = t / L;                          // sink slot of the gravity loop
-    const int lane = t % L;
-    const bool has = k < it.nsink;
-    const int i = it.sink0 + (has ? k : 0);       // inactive slots shadow sink 0 (results unused)
-    const int gbase = (t & 31) & ~(L - 1);        // first lane of the sink's group in the warp
 
-    // ---- batch of independent loads ----
-    // first source tile, in registers until stored to shared memory
+    // ---- first source tile, into registers ----
     float4 th = make_float4(0.f, 0.f, 0.f, 0.f), tl = th;
     D4 td{0.0, 0.0, 0.0, 0.0};
     int tid = 0;
-    auto fetch = [&](int j0) {
-        const int nj = min(kTile, it.src1 - j0);
-        if (t < nj) {
-            const int j = j0 + t;
-            if (kF32) {
-                th = P.pos_hi_in[j];
-                if (MODE == MODE_MIXED) tl = P.pos_lo_in[j];
-            } else {
-                tid = P.id[j];
-                const double m = P.mass[j];
-                td = D4{P.r_in[3 * j], P.r_in[3 * j + 1], P.r_in[3 * j + 2], (MODE == MODE_FP64 && tid < 0) ? 0.0 : m};
-            }
-        }
-    };
-    auto stash = [&]() {
+    if (t < min(kTile, it.src1 - it.src0)) {
+        const int j = it.src0 + t;
         if (kF32) {
-            sm.src.f.hi[t] = th;
-            if (MODE == MODE_MIXED) sm.src.f.lo[t] = tl;
+            th = P.pos_hi_in[j];
+            if (MODE == MODE_MIXED) tl = P.pos_lo_in[j];
         } else {
-            sm.src.d.d[t] = td;
-            sm.src.d.id[t] = tid;
+            tid = P.id[j];
+            const double m = P.mass[j];
+            td = D4{P.r_in[3 * j], P.r_in[3 * j + 1], P.r_in[3 * j + 2], (MODE == MODE_FP64 && tid < 0) ? 0.0 : m};
         }
-    };
-    if (it.src0 < it.src1) fetch(it.src0);
-
-    // the sink of the gravity loop
-    float4 H = make_float4(0.f, 0.f, 0.f, 0.f), Lo = H;
-    double xi = 0.0, yi = 0.0, zi = 0.0;
-    if (kF32) {
-        H = P.pos_hi_in[i];
-        if (MODE == MODE_MIXED) Lo = P.pos_lo_in[i];
-    } else {
-        xi = P.r_in[3 * i];
-        yi = P.r_in[3 * i + 1];
-        zi = P.r_in[3 * i + 2];
     }
 
-    // the element of the epilogue
+    // ---- the element of the epilogue; its operands go to shared memory ----
     const int nel = 3 * it.nsink;
     const bool elem = t < nel;
     const int ke = elem ? t / 3 : 0;
@@ -172,43 +348,25 @@ __global__ void __launch_bounds__(kTile) k_stage(const StageParams P)
     const int idi = P.id[ie];
     const double rc = P.r_in[x];
     const bool drag_on = P.gas.enabled && it.cls == CLS_NSI;
-    const bool need_vs = drag_on || (!P.standalone && V != 0);
-    const double vs = need_vs ? P.Kr[s][x] : 0.0;    // stage velocity of the element
-    double yr = 0.0, yv = 0.0;
-    double kr[9], kv[9];
-#pragma unroll
-    for (int q = 0; q < 9; q++) kr[q] = kv[q] = 0.0;
-    if constexpr (kRkf) {
-        yr = P.y_r[x];
-        yv = P.y_v[x];
-#pragma unroll
-        for (int q = 0; q < kNnz[V]; q++) {
-            kr[q] = P.Kr[kSrc[V][q]][x];
-            if (kSrc[V][q] != V - 1) kv[q] = P.Kv[kSrc[V][q]][x];
+    const bool need_vs = drag_on || V != 0;
+    if (elem) {
+        if (need_vs) cp_async8(&ops[O::VS][t], P.Kr[s] + x);
+        if constexpr (V >= 1 && V <= 14) {
+            cp_async8(&ops[O::YR][t], P.y_r + x);
+            cp_async8(&ops[O::YV][t], P.y_v + x);
+            if (ce == 0) {
+                cp_async8(&ops[O::M][t], P.mass + ie);
+                cp_async8(&ops[O::RAD][t], P.radius + ie);
+            }
         }
-    } else if constexpr (V == 13) {
-        yr = P.y_r[x];
-        yv = P.y_v[x];
-    } else if constexpr (V == 14) {
-        yr = P.y_r[x];
-        yv = P.y_v[x];
 #pragma unroll
-        for (int q = 0; q < 3; q++) {
-            kr[q] = P.Kr[q][x];
-            kv[q] = P.Kv[q][x];
+        for (int q = 0; q < O::nk; q++) {
+            const int src = op_src<V>(q);
+            cp_async8(&ops[O::KR + q][t], P.Kr[src] + x);
+            if (!(kRkf && src == V - 1)) cp_async8(&ops[O::KV + q][t], P.Kv[src] + x);
         }
-    } else if constexpr (V == 15) {
-        kr[0] = P.Kr[0][x]; kr[1] = P.Kr[10][x]; kr[2] = P.Kr[11][x];
-        kv[0] = P.Kv[0][x]; kv[1] = P.Kv[10][x]; kv[2] = P.Kv[11][x];
-    } else if constexpr (V == 16) {
-        kr[0] = P.Kr[3][x];
-        kv[0] = P.Kv[3][x];
     }
-    double m_i = 0.0, rad_i = 0.0;
-    if (V != 0 && V <= 14 && ce == 0) {
-        m_i = P.mass[ie];
-        rad_i = P.radius[ie];
-    }
+    cp_async_commit();
 
     // ---- drag factor and star factors: scalars per sink, thread t < nsink ----
     const bool star_term = kF32 && it.nstar > 0;
@@ -256,7 +414,13 @@ __global__ void __launch_bounds__(kTile) k_stage(const StageParams P)
 #pragma unroll
     for (int q = 0; q < kStarBatch; q++) sp[q] = q < nst0 ? P.r_in[3 * (it.soff + q) + ce] : 0.0;
     if (star_term) star_factors(0, nst0);
-    if (it.src0 < it.src1) stash();
+    if (kF32) {
+        sm.src.f.hi[t] = th;
+        if (MODE == MODE_MIXED) sm.src.f.lo[t] = tl;
+    } else {
+        sm.src.d.d[t] = td;
+        sm.src.d.id[t] = tid;
+    }
     __syncthreads();
     double sc_sum = 0.0;
     if (star_term) {
@@ -272,122 +436,24 @@ __global__ void __launch_bounds__(kTile) k_stage(const StageParams P)
         }
     }
 
-    // ---- gravity of the chunk's sources; the next tile is fetched while the
-    // current one is in use ----
-    double ax = 0.0, ay = 0.0, az = 0.0;
-    if (kF32) {
-        float sxh = 0.f, sxl = 0.f, syh = 0.f, syl = 0.f, szh = 0.f, szl = 0.f;
-        for (int j0 = it.src0; j0 < it.src1; j0 += kTile) {
-            const int nj = min(kTile, it.src1 - j0);
-            const bool more = j0 + kTile < it.src1;
-            if (more) fetch(j0 + kTile);
-            if (has) {
-                float tx = 0.f, ty = 0.f, tz = 0.f;
-#pragma unroll 4
-                for (int jj = lane; jj < nj; jj += L) {
-                    const float4 h = sm.src.f.hi[jj];
-                    float dx, dy, dz;
-                    if (MODE == MODE_MIXED) {
-                        const float4 l = sm.src.f.lo[jj];
-                        dx = (h.x - H.x) + (l.x - Lo.x);
-                        dy = (h.y - H.y) + (l.y - Lo.y);
-                        dz = (h.z - H.z) + (l.z - Lo.z);
-                    } else {
-                        dx = h.x - H.x;
-                        dy = h.y - H.y;
-                        dz = h.z - H.z;
-                    }
-                    const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, kEps2)));
-                    const float ri = rsqrtf(r2);
-                    const float ri2 = ri * ri;
-                    const float sc = h.w * ri * ri2;
-                    tx = fmaf(sc, dx, tx);
-                    ty = fmaf(sc, dy, ty);
-                    tz = fmaf(sc, dz, tz);
-                }
-                ds_add(sxh, sxl, tx);
-                ds_add(syh, syl, ty);
-                ds_add(szh, szl, tz);
-            }
-            if (more) {
-                __syncthreads();
-                stash();
-                __syncthreads();
-            }
-        }
-        // lanes -> one double-single sum (TwoSum in FP32, a fixed butterfly), then lane c
-        // converts component c to FP64
-        for (int o = 1; o < L; o <<= 1) {
-            ds_merge(sxh, sxl, __shfl_xor_sync(0xffffffffu, sxh, o), __shfl_xor_sync(0xffffffffu, sxl, o));
-            ds_merge(syh, syl, __shfl_xor_sync(0xffffffffu, syh, o), __shfl_xor_sync(0xffffffffu, syl, o));
-            ds_merge(szh, szl, __shfl_xor_sync(0xffffffffu, szh, o), __shfl_xor_sync(0xffffffffu, szl, o));
-        }
-        const int cl = lane < 3 ? lane : 0;
-        const float hh = cl == 0 ? sxh : (cl == 1 ? syh : szh);
-        const float ll = cl == 0 ? sxl : (cl == 1 ? syl : szl);
-        const double v = lane < 3 ? (double)hh + (double)ll : 0.0;
-        ax = ay = az = v;   // lane c holds component c in all three
+    // ---- gravity of the chunk's sources ----
+    double mine;
+    int mine_k;
+    bool mine_ok;
+    if constexpr (kF32) {
+        if (it.spt == 2) gravity_f32<MODE, 2>(sm, P, it, th, tl, mine, mine_k, mine_ok);
+        else gravity_f32<MODE, 1>(sm, P, it, th, tl, mine, mine_k, mine_ok);
     } else {
-        for (int j0 = it.src0; j0 < it.src1; j0 += kTile) {
-            const int nj = min(kTile, it.src1 - j0);
-            const bool more = j0 + kTile < it.src1;
-            if (more) fetch(j0 + kTile);
-            if (has) {
-                if (MODE == MODE_FP64_EXACT) {
-                    // calc_grav_accel_naive, pp_disk.cu:389-413, bit for bit: lane 0 alone,
-                    // sources in index order
-                    if (lane == 0) {
-                        for (int jj = 0; jj < nj; jj++) {
-                            const D4 q = sm.src.d.d[jj];
-                            if (j0 + jj == i || 0 > sm.src.d.id[jj]) continue;
-                            const double dx = __dsub_rn(q.x, xi), dy = __dsub_rn(q.y, yi), dz = __dsub_rn(q.z, zi);
-                            double w = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-                            const double d = __dsqrt_rn(w);
-                            w = __ddiv_rn(q.w, __dmul_rn(d, w));
-                            ax = __dadd_rn(ax, __dmul_rn(w, dx));
-                            ay = __dadd_rn(ay, __dmul_rn(w, dy));
-                            az = __dadd_rn(az, __dmul_rn(w, dz));
-                        }
-                    }
-                } else {
-                    for (int jj = lane; jj < nj; jj += L) {
-                        const D4 q = sm.src.d.d[jj];
-                        const double dx = q.x - xi, dy = q.y - yi, dz = q.z - zi;
-                        const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
-                        double ri = rsqrt(r2);
-                        ri = r2 > 0.0 ? ri : 0.0;
-                        const double sc = q.w * ri * ri * ri;
-                        ax = fma(sc, dx, ax);
-                        ay = fma(sc, dy, ay);
-                        az = fma(sc, dz, az);
-                    }
-                }
-            }
-            if (more) {
-                __syncthreads();
-                stash();
-                __syncthreads();
-            }
-        }
-        if (MODE == MODE_FP64_EXACT) {
-            ax = __shfl_sync(0xffffffffu, ax, gbase);
-            ay = __shfl_sync(0xffffffffu, ay, gbase);
-            az = __shfl_sync(0xffffffffu, az, gbase);
-        } else {
-            ax = group_sum(ax, L);
-            ay = group_sum(ay, L);
-            az = group_sum(az, L);
-        }
+        gravity_f64<MODE>(sm, P, it, td, tid, mine, mine_k, mine_ok);
     }
-    // lane c of each sink holds component c
-    const double mine = lane == 0 ? ax : (lane == 1 ? ay : az);
+    const int mine_c = (t % it.lanes) % 3;
 
     // ---- source chunks of one sink tile -> the CTA that finishes last sums them,
     // every thread of it on a contiguous range of chunks, in a fixed order ----
     double a = 0.0;
     if (it.nchunk > 1) {
-        if (has && lane < 3) {
-            double* p = P.partial + 3 * ((long long)it.part_off + (long long)it.chunk * it.nsink) + 3 * k + lane;
+        if (mine_ok) {
+            double* p = P.partial + 3 * ((long long)it.part_off + (long long)it.chunk * it.nsink) + 3 * mine_k + mine_c;
             *p = mine;
         }
         __threadfence();
@@ -397,7 +463,10 @@ __global__ void __launch_bounds__(kTile) k_stage(const StageParams P)
             sm.flag = (prev == (unsigned)(it.nchunk - 1));
         }
         __syncthreads();
-        if (!sm.flag) return;   // uniform
+        if (!sm.flag) {        // uniform
+            cp_async_wait_all();   // no copy may land in shared memory after the CTA has gone
+            return;
+        }
         __threadfence();
         const int nsplit = kTile / nel;
         const int sp_i = t / nel;
@@ -414,13 +483,15 @@ __global__ void __launch_bounds__(kTile) k_stage(const StageParams P)
             for (int q = 0; q < nsplit; q++) a += sm.acc[q * nel + t];
         if (t == 0) P.tile_cnt[it.tile] = 0u;
     } else {
-        if (has && lane < 3) sm.acc[3 * k + lane] = mine;
+        if (mine_ok) sm.acc[3 * mine_k + mine_c] = mine;
         __syncthreads();
         if (elem) a = sm.acc[t];
     }
+    cp_async_wait_all();
     if (!elem) return;
 
     // ---- element-wise FP64 epilogue ----
+    const double vs = need_vs ? ops[O::VS][t] : 0.0;   // stage velocity of the element
     if (star_term) a = sc_sum + a;
     if (!(idi > 0)) a = 0.0;   // calc_grav_accel_naive zeroes inactive sinks (pp_disk.cu:386-388)
     if (drag_act) {
@@ -430,19 +501,20 @@ __global__ void __launch_bounds__(kTile) k_stage(const StageParams P)
     P.Kv[s][x] = a;
 
     if constexpr (V >= 1 && V <= 14) {
+        const double yr = ops[O::YR][t], yv = ops[O::YV][t];
         double orr, ovv;
         if constexpr (kRkf) {
             // ytemp of stage V: y + dt * sum_q a_{V,q} K_q, terms in red's order
             // (rk8_kernel::calc_ytemp_for_f1..f12, int_rungekutta8.cu:80-246)
             constexpr int off = 1 + V * (V - 1) / 2;
-            if (kSrc[V][0] == V - 1) kv[0] = a;
-            double ar = mul<EXACT>(c_tb.a[off + kSrc[V][0]], kr[0]);
-            double av = mul<EXACT>(c_tb.a[off + kSrc[V][0]], kv[0]);
+            const double kv0 = (kSrc[V][0] == V - 1) ? a : ops[O::KV][t];
+            double ar = mul<EXACT>(c_tb.a[off + kSrc[V][0]], ops[O::KR][t]);
+            double av = mul<EXACT>(c_tb.a[off + kSrc[V][0]], kv0);
 #pragma unroll
-            for (int q = 1; q < kNnz[V]; q++) {
+            for (int q = 1; q < O::nk; q++) {
                 const double aq = c_tb.a[off + kSrc[V][q]];
-                const double kvq = (kSrc[V][q] == V - 1) ? a : kv[q];
-                ar = madd<EXACT>(ar, aq, kr[q]);
+                const double kvq = (kSrc[V][q] == V - 1) ? a : ops[O::KV + q][t];
+                ar = madd<EXACT>(ar, aq, ops[O::KR + q][t]);
                 av = madd<EXACT>(av, aq, kvq);
             }
             orr = madd<EXACT>(yr, dt, ar);
@@ -455,15 +527,15 @@ __global__ void __launch_bounds__(kTile) k_stage(const StageParams P)
         } else {
             // RK4 y_{n+1} as the positions of the adaptive stage 4
             const double b0 = mul<EXACT>(c_tb.b4[0], dt), b1 = mul<EXACT>(c_tb.b4[1], dt);
-            orr = rk4_ynp1<EXACT>(yr, b0, b1, kr[0], kr[1], kr[2], vs);
-            ovv = rk4_ynp1<EXACT>(yv, b0, b1, kv[0], kv[1], kv[2], a);
+            orr = rk4_ynp1<EXACT>(yr, b0, b1, ops[O::KR][t], ops[O::KR + 1][t], ops[O::KR + 2][t], vs);
+            ovv = rk4_ynp1<EXACT>(yv, b0, b1, ops[O::KV][t], ops[O::KV + 1][t], ops[O::KV + 2][t], a);
         }
         P.r_out[x] = orr;
         P.Kr[P.next][x] = ovv;
         write_pos_c(P.pos_hi_out, P.pos_lo_out, ie, ce, orr);
         if (ce == 0) {
-            reinterpret_cast<float*>(P.pos_hi_out + ie)[3] = __double2float_rn(idi >= 0 ? m_i : 0.0);
-            reinterpret_cast<float*>(P.pos_lo_out + ie)[3] = __double2float_rn(rad_i);
+            reinterpret_cast<float*>(P.pos_hi_out + ie)[3] = __double2float_rn(idi >= 0 ? ops[O::M][t] : 0.0);
+            reinterpret_cast<float*>(P.pos_lo_out + ie)[3] = __double2float_rn(ops[O::RAD][t]);
         }
     } else if constexpr (V == 15 || V == 16) {
         double e = 0.0;
@@ -471,12 +543,12 @@ __global__ void __launch_bounds__(kTile) k_stage(const StageParams P)
             double er, ev;
             if constexpr (V == 15) {
                 // rk8_kernel::calc_error, int_rungekutta8.cu:248-260
-                er = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(kr[0], kr[1]), kr[2]), vs));
-                ev = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(kv[0], kv[1]), kv[2]), a));
+                er = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(ops[O::KR][t], ops[O::KR + 1][t]), ops[O::KR + 2][t]), vs));
+                ev = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(ops[O::KV][t], ops[O::KV + 1][t]), ops[O::KV + 2][t]), a));
             } else {
                 // rk4_kernel::calc_error, int_rungekutta4.cu:62-73
-                er = fabs(kr[0] - vs);
-                ev = fabs(kv[0] - a);
+                er = fabs(ops[O::KR][t] - vs);
+                ev = fabs(ops[O::KV][t] - a);
             }
             e = fmax(er, ev);
             if (er != er || ev != ev) e = __longlong_as_double(0x7ff8000000000000ll);

@@ -191,8 +191,9 @@ def config4_system(i, n_min=128, n_max=4096):
                         pl_mass=EARTH_TO_SOLAR / n_pl)
 
 
-def config4(n_systems=512, n_min=128, n_max=4096):
-    return [config4_system(i, n_min, n_max) for i in range(n_systems)]
+def config4(n_systems=512, n_min=128, n_max=4096, first=0):
+    """Systems first .. first + n_systems - 1 of the ensemble."""
+    return [config4_system(first + i, n_min, n_max) for i in range(n_systems)]
 
 
 def gas_disk_config3():

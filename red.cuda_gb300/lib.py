@@ -258,20 +258,33 @@ class Sim:
         _check(load().red_calc_energy_interacting(self.h, sys, _p(out)))
         return out
 
-    def get_state(self, sys=0):
+    def get_state(self, sys=0, out=None, parts="rvpm"):
+        """System `sys` as a System; with `out`, the arrays named in `parts`
+        (r, v, p, m = metadata) are written into out's arrays in place (which
+        must be contiguous and hold n_total records) and out is returned."""
         info = self.info(sys)
         n = info.n_total
-        r, v, p, md = np.zeros(n, VAR4), np.zeros(n, VAR4), np.zeros(n, PARAM), np.zeros(n, BMD)
-        _check(load().red_get_state(self.h, sys, _p(r), _p(v), _p(p), _p(md)))
+        if out is None:
+            r, v, p, md = np.zeros(n, VAR4), np.zeros(n, VAR4), np.zeros(n, PARAM), np.zeros(n, BMD)
+        else:
+            r, v, p, md = out.r, out.v, out.p, out.md
+            for a in (r, v, p, md):
+                if not a.flags["C_CONTIGUOUS"] or len(a) != n:
+                    raise ValueError("out arrays must be contiguous with %d records" % n)
+        ptr = [_p(a) if k in parts else None for a, k in ((r, "r"), (v, "v"), (p, "p"), (md, "m"))]
+        _check(load().red_get_state(self.h, sys, *ptr))
+        if out is not None:
+            return out
         s = System(r, v, p, md, np.array(info.playing, np.uint32))
         s.inactive = np.array(info.inactive, np.uint32)
         s.removed = np.array(info.removed, np.uint32)
         return s
 
-    def set_state(self, sys, s):
-        _check(load().red_set_state(self.h, sys, _p(np.ascontiguousarray(s.r, VAR4)),
-                                    _p(np.ascontiguousarray(s.v, VAR4)), _p(np.ascontiguousarray(s.p, PARAM)),
-                                    _p(np.ascontiguousarray(s.md, BMD))))
+    def set_state(self, sys, s, parts="rvpm"):
+        """Writes the arrays of System s named in `parts` (r, v, p, m = metadata)."""
+        arrs = [(s.r, VAR4, "r"), (s.v, VAR4, "v"), (s.p, PARAM, "p"), (s.md, BMD, "m")]
+        keep = [np.ascontiguousarray(a, t) if k in parts else None for a, t, k in arrs]
+        _check(load().red_set_state(self.h, sys, *[_p(a) if a is not None else None for a in keep]))
 
     def set_dt_next(self, sys, dt):
         _check(load().red_set_dt_next(self.h, sys, dt))
