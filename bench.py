@@ -303,10 +303,7 @@ def run_ours(args, rg, rank, world, local_rank):
     value = inter * world / (t_max * 1e-3)
     sim_years = sim_dt / K_GAUSS / YEAR
     # roofline of the dominant kernel (kernel-by-kernel tries, CUDA events)
-    traffic = {}
     try:
-        for ln in open(os.path.join(ROOT, "profiles", "traffic.json")):
-            pass
         traffic = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(args.config, {})
     except (OSError, ValueError):
         traffic = {}
