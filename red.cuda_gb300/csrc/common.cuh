@@ -50,6 +50,44 @@ __device__ __forceinline__ void ds_merge(float& ah, float& al, float bh, float b
     al = al + bl + e;
 }
 
+// Double-single numbers as float2 (x = hi, y = lo, hi + lo the value, |lo| <=
+// ulp(hi) after renormalisation): Dekker (1971) and Knuth's TwoSum, the
+// product's error term from fmaf.  About 48 significant bits.
+__device__ __forceinline__ float2 dsn(float hi, float lo) { return make_float2(hi, lo); }
+__device__ __forceinline__ float2 dsn_norm(float a, float b)
+{
+    float s, e;
+    two_sum(a, b, s, e);
+    return make_float2(s, e);
+}
+__device__ __forceinline__ float2 dsn_add(float2 a, float2 b)
+{
+    float s, e;
+    two_sum(a.x, b.x, s, e);
+    return dsn_norm(s, e + (a.y + b.y));
+}
+__device__ __forceinline__ float2 dsn_sub(float2 a, float2 b) { return dsn_add(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 dsn_mul(float2 a, float2 b)
+{
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, fmaf(a.y, b.x, e));
+    return dsn_norm(p, e);
+}
+// 1 / sqrt(x) for x > 0: the hardware estimate refined by two Newton steps
+// y <- y + y (1 - x y^2) / 2, the second in double-single arithmetic.
+__device__ __forceinline__ float2 dsn_rsqrt(float2 x)
+{
+    const float y = rsqrtf(x.x);
+    const float2 t = dsn_mul(x, dsn_norm(y * y, fmaf(y, y, -(y * y))));
+    const float r = (1.0f - t.x) - t.y;
+    const float2 y1 = dsn_norm(y, 0.5f * y * r);
+    const float2 r1 = dsn_sub(make_float2(1.0f, 0.0f), dsn_mul(x, dsn_mul(y1, y1)));
+    const float2 c = dsn_mul(y1, r1);
+    return dsn_add(y1, make_float2(0.5f * c.x, 0.5f * c.y));
+}
+__device__ __forceinline__ double dsn_to_double(float2 a) { return (double)a.x + (double)a.y; }
+
 __device__ __forceinline__ void split_ds(double x, float& h, float& l)
 {
     h = __double2float_rn(x);

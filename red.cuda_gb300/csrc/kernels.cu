@@ -17,15 +17,22 @@ namespace redgb {
 // ---------------------------------------------------------------------------
 // per-body kernels
 // ---------------------------------------------------------------------------
+// FP32 copies of y_r for stage 0 (buffer 0), and the mass / radius words of
+// both stage buffers: the stage kernels write only x, y, z, so the .w words
+// set here hold until the next host update of the bodies.
 __global__ void __launch_bounds__(kSegment) k_prep(const Segment* segs, const SysInfo* sinfo, const DevSys* sys,
                                                    const double* y_r, const double* mass, const double* radius,
-                                                   const int* id, float4* hi, float4* lo, int all)
+                                                   const int* id, float4* hi, float4* lo, float4* hi1, float4* lo1,
+                                                   int all)
 {
     const Segment sg = segs[blockIdx.x];
     if (!all && !runnable(sys[sg.sys])) return;
     const int i = sg.b0 + threadIdx.x;
     if (i >= sg.b1) return;
-    write_pos(hi, lo, i, y_r[3 * i], y_r[3 * i + 1], y_r[3 * i + 2], id[i] >= 0 ? mass[i] : 0.0, radius[i]);
+    const double m_eff = id[i] >= 0 ? mass[i] : 0.0;
+    write_pos(hi, lo, i, y_r[3 * i], y_r[3 * i + 1], y_r[3 * i + 2], m_eff, radius[i]);
+    reinterpret_cast<float*>(hi1 + i)[3] = __double2float_rn(m_eff);
+    reinterpret_cast<float*>(lo1 + i)[3] = __double2float_rn(radius[i]);
 }
 
 // One thread per system: integrator::step's accept / reject logic
@@ -89,11 +96,7 @@ __global__ void __launch_bounds__(4 * kFinishBodies) k_finish(const FinishParams
     const bool acc = S->accepted;
     if (!acc && !runnable(*S)) return;
     if (i >= sg.b1) return;
-    if (c == 3) {
-        reinterpret_cast<float*>(P.pos_hi0 + i)[3] = __double2float_rn(P.id[i] >= 0 ? P.mass[i] : 0.0);
-        reinterpret_cast<float*>(P.pos_lo0 + i)[3] = __double2float_rn(P.radius[i]);
-        return;
-    }
+    if (c == 3) return;   // the .w words (mass, radius) are set by k_prep
     const int x = 3 * i + c;
     double r;
     if (acc) {
@@ -239,7 +242,9 @@ __global__ void __launch_bounds__(kSegment) k_grid_insert(const CollParams P)
 // Half of the neighbourhood: the own cell (pairs with j > i) and the 13 cells
 // of the forward half-space, so that every unordered pair of small bodies in
 // neighbouring cells is seen once; the pair is tested as (min, max) like red's
-// i < j loop.  The 14 bucket heads are loaded before any list is walked.
+// i < j loop.  The 14 bucket lists are walked side by side: each round loads
+// the current element of every list at once, so a thread needs as many
+// dependent memory round trips as its longest list, not their sum.
 __global__ void __launch_bounds__(kSegment) k_grid_query(const CollParams P)
 {
     const Segment sg = P.segs[blockIdx.x];
@@ -251,8 +256,9 @@ __global__ void __launch_bounds__(kSegment) k_grid_query(const CollParams P)
     if (i >= sg.b1 || i < si.off + si.n_SI) return;
     const double f = P.factor * P.factor;
     const int4 c = P.cell[i];
-    int head[14];
-    int4 nb[14];
+    constexpr int kNb = 14;
+    int cur[kNb];
+    int4 nb[kNb];
     int q = 0;
 #pragma unroll
     for (int dz = 0; dz <= 1; dz++)
@@ -263,17 +269,32 @@ __global__ void __launch_bounds__(kSegment) k_grid_query(const CollParams P)
                 const bool fwd = dz > 0 || (dz == 0 && (dy > 0 || (dy == 0 && dx >= 0)));
                 if (!fwd) continue;
                 nb[q] = make_int4(c.x + dx, c.y + dy, c.z + dz, 0);
-                head[q] = __ldcg(P.head + g.toff + bucket_of(nb[q].x, nb[q].y, nb[q].z, g.mask));
+                cur[q] = __ldcg(P.head + g.toff + bucket_of(nb[q].x, nb[q].y, nb[q].z, g.mask));
                 q++;
             }
+    // a list is at most as long as the system's small-body count: the bound ends every walk
+    const int bound = si.n - si.n_SI;
+    bool any = true;
+    for (int round = 0; any && round <= bound; round++) {
+        int4 cj[kNb];
+        int nx[kNb];
 #pragma unroll
-    for (int b = 0; b < 14; b++) {
-        int j = head[b];
-        while (j >= 0) {
-            const int4 cj = P.cell[j];
-            if (cj.x == nb[b].x && cj.y == nb[b].y && cj.z == nb[b].z && (b != 0 || j > i))
-                collide_exact(P, S, sg.sys, min(i, j), max(i, j), f);
-            j = __ldcg(P.next + j);
+        for (int b = 0; b < kNb; b++) {
+            if (cur[b] >= 0) {
+                cj[b] = P.cell[cur[b]];
+                nx[b] = __ldcg(P.next + cur[b]);
+            }
+        }
+        any = false;
+#pragma unroll
+        for (int b = 0; b < kNb; b++) {
+            if (cur[b] >= 0) {
+                const int j = cur[b];
+                if (cj[b].x == nb[b].x && cj[b].y == nb[b].y && cj[b].z == nb[b].z && (b != 0 || j > i))
+                    collide_exact(P, S, sg.sys, min(i, j), max(i, j), f);
+                cur[b] = nx[b];
+                any = any || nx[b] >= 0;
+            }
         }
     }
 }
@@ -426,10 +447,10 @@ void launch_stage(const StageParams& P, int n_items, int mode, cudaStream_t s)
 }
 
 void launch_prep(const Segment* segs, int n_segs, const SysInfo* sinfo, const DevSys* sys, const double* y_r,
-                 const double* mass, const double* radius, const int* id, float4* hi, float4* lo, int all,
-                 cudaStream_t s)
+                 const double* mass, const double* radius, const int* id, float4* hi, float4* lo, float4* hi1,
+                 float4* lo1, int all, cudaStream_t s)
 {
-    if (n_segs > 0) k_prep<<<n_segs, kSegment, 0, s>>>(segs, sinfo, sys, y_r, mass, radius, id, hi, lo, all);
+    if (n_segs > 0) k_prep<<<n_segs, kSegment, 0, s>>>(segs, sinfo, sys, y_r, mass, radius, id, hi, lo, hi1, lo1, all);
 }
 
 void launch_control(const ControlParams& P, cudaStream_t s)

@@ -24,7 +24,7 @@
 #include <vector>
 
 #include "redgb_dev.cuh"
-#include "../../include/redgb.h"
+#include "redgb.h"
 
 using namespace redgb;
 
@@ -104,7 +104,7 @@ extern "C" int red_calc_accel_noalloc(const red_accel_args_t* a)
     std::vector<GravItem> items;
     size_t part = 0;
     int tiles = 0;
-    plan_gravity_items(si, 0, a->precision, 0, 32, items, part, tiles);
+    plan_gravity_items(si, 0, a->precision, 0, 32, count_sink_tiles(si, a->precision, 32), items, part, tiles);
     const size_t off_part = ((kOffPos + 2 * pos_bytes + 255) / 256) * 256;
     if (items.size() > kMaxItems || (size_t)tiles > kMaxTiles || off_part + part * 3 * sizeof(double) > kScratchBytes)
         return fail(RED_ERR_ARG, "red_calc_accel_noalloc: the launch plan does not fit the scratch array");

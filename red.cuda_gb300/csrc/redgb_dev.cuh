@@ -222,7 +222,10 @@ struct EjhcParams {
 };
 
 // Host-side plan of the stage kernel for one system (sim.cu).
-void plan_gravity_items(const SysInfo& si, int sys, int mode, int chunk_override, int lanes_cap,
+// tiles_all: sink tiles of every system planned into the same launch (count_sink_tiles).
+constexpr int kBatchRecords = 16;   // partial records loaded per batch by the reducing CTA
+int count_sink_tiles(const SysInfo& si, int mode, int lanes_cap);
+void plan_gravity_items(const SysInfo& si, int sys, int mode, int chunk_override, int lanes_cap, int tiles_all,
                         std::vector<GravItem>& items, size_t& part, int& tiles);
 
 // Host-side launchers (kernels.cu, stage_*.cu).  The stage kernel's mode
@@ -240,8 +243,8 @@ void launch_stage_fp32(const StageParams& P, int n, int variant, cudaStream_t s)
 void launch_stage_fp64(const StageParams& P, int n, int variant, cudaStream_t s);
 void launch_stage_exact(const StageParams& P, int n, int variant, cudaStream_t s);
 void launch_prep(const Segment* segs, int n_segs, const SysInfo* sinfo, const DevSys* sys, const double* y_r,
-                 const double* mass, const double* radius, const int* id, float4* hi, float4* lo, int all,
-                 cudaStream_t s);
+                 const double* mass, const double* radius, const int* id, float4* hi, float4* lo, float4* hi1,
+                 float4* lo1, int all, cudaStream_t s);
 void launch_control(const ControlParams& P, cudaStream_t s);
 void launch_finish(const FinishParams& P, int n_segs, cudaStream_t s);
 void launch_collision(const CollParams& P, int n_items, int n_segs, bool use_grid, size_t table_size,

@@ -19,7 +19,7 @@
 #include <vector>
 
 #include "redgb_dev.cuh"
-#include "../../include/redgb.h"
+#include "redgb.h"
 
 using namespace redgb;
 
@@ -143,35 +143,68 @@ namespace redgb {
 // CTAs of the stage kernel for one system: sink tiles of the SI, NSI and NI
 // classes (red_type.h:670-692), each split into source chunks; appends to
 // items and advances the partial-record and tile counters.
-void plan_gravity_items(const SysInfo& si, int s, int mode, int chunk_override, int lanes_cap,
-                        std::vector<GravItem>& items, size_t& part, int& tiles)
+// The gravity classes of one system: sinks [s0, s1) against sources [j0, j1)
+// (body indices relative to the system), red's interaction bounds
+// (red_type.h:670-692); the FP32 modes take the stars out of the sources (their
+// term is added in FP64 by the epilogue).
+struct GravClass { int cls, s0, s1, j0, j1; };
+static void gravity_classes(const SysInfo& si, int mode, GravClass out[3])
 {
-    // enough CTAs for several waves of ~6 resident CTAs on each of GB300's 152 SMs
-    const int kTargetCtas = 8 * 6 * 152;
     const bool fp32 = (mode == MODE_MIXED || mode == MODE_FP32);
     const int src_start = fp32 ? si.n_star : 0;
-    struct C { int cls, s0, s1, j0, j1; };
-    const C cls[3] = {{CLS_SI, 0, si.n_SI, src_start, si.n_massive},
-                      {CLS_NSI, si.n_SI, si.n_massive, src_start, si.n_SI},
-                      {CLS_NI, si.n_massive, si.n, src_start, si.n_massive}};
-    for (const C& q : cls) {
+    out[0] = {CLS_SI, 0, si.n_SI, src_start, si.n_massive};
+    out[1] = {CLS_NSI, si.n_SI, si.n_massive, src_start, si.n_SI};
+    out[2] = {CLS_NI, si.n_massive, si.n, src_start, si.n_massive};
+}
+
+// Threads per sink group and sinks per group of one class: a power of two in
+// [4, 32] lanes.  Many sinks in the FP32 modes: 8 lanes serving 2 sinks each
+// (each source read feeds two interactions).  Few sinks: more lanes, the more
+// the longer the source list.
+static void class_shape(int mode, int nsink_all, int nsrc, int lanes_cap, int& lanes, int& spt)
+{
+    const bool fp32 = (mode == MODE_MIXED || mode == MODE_FP32);
+    lanes = 4;
+    spt = 1;
+    if (mode == MODE_FP64_EXACT) return;
+    if (fp32 && nsink_all >= 32 && lanes_cap >= 8) {
+        lanes = 8;
+        spt = 2;
+        return;
+    }
+    while (lanes < 32 && lanes < lanes_cap && (2 * lanes * nsink_all <= kTile || 256 * 2 * lanes <= nsrc)) lanes *= 2;
+}
+
+int count_sink_tiles(const SysInfo& si, int mode, int lanes_cap)
+{
+    GravClass cls[3];
+    gravity_classes(si, mode, cls);
+    int n = 0;
+    for (const GravClass& q : cls) {
+        const int nsink_all = q.s1 - q.s0;
+        if (nsink_all <= 0) continue;
+        int lanes, spt;
+        class_shape(mode, nsink_all, std::max(0, q.j1 - q.j0), lanes_cap, lanes, spt);
+        const int tile_sinks = kTile / lanes * spt;
+        n += (nsink_all + tile_sinks - 1) / tile_sinks;
+    }
+    return n;
+}
+
+void plan_gravity_items(const SysInfo& si, int s, int mode, int chunk_override, int lanes_cap, int tiles_all,
+                        std::vector<GravItem>& items, size_t& part, int& tiles)
+{
+    // the launch should hold several waves of CTAs (6 resident on each of
+    // GB300's 152 SMs); tiles_all counts the sink tiles of every system in it
+    const int kTargetCtas = 8 * 6 * 152;
+    GravClass cls[3];
+    gravity_classes(si, mode, cls);
+    for (const GravClass& q : cls) {
         const int nsink_all = q.s1 - q.s0;
         if (nsink_all <= 0) continue;
         const int nsrc = std::max(0, q.j1 - q.j0);
-        // threads per sink group: a power of two in [4, 32].  Many sinks in the FP32
-        // modes: 8 lanes serving 2 sinks each (each source read feeds two
-        // interactions).  Few sinks: more lanes, the more the longer the source list.
-        int lanes = 4, spt = 1;
-        if (mode != MODE_FP64_EXACT) {
-            if (fp32 && nsink_all >= 32 && lanes_cap >= 8) {
-                lanes = 8;
-                spt = 2;
-            } else {
-                while (lanes < 32 && lanes < lanes_cap &&
-                       (2 * lanes * nsink_all <= kTile || 256 * 2 * lanes <= nsrc))
-                    lanes *= 2;
-            }
-        }
+        int lanes, spt;
+        class_shape(mode, nsink_all, nsrc, lanes_cap, lanes, spt);
         const int tile_sinks = kTile / lanes * spt;
         const int ntile = (nsink_all + tile_sinks - 1) / tile_sinks;
         for (int t = 0; t < ntile; t++) {
@@ -179,21 +212,21 @@ void plan_gravity_items(const SysInfo& si, int s, int mode, int chunk_override, 
             const int nsink = std::min(tile_sinks, q.s1 - s0);
             int chunk = std::max(nsrc, 1);
             if (mode != MODE_FP64_EXACT) {
-                int c;
                 if (chunk_override > 0) {
-                    c = chunk_override;
+                    chunk = chunk_override;
                 } else {
-                    // enough CTAs to fill the SMs several times over, but at least
-                    // kMinIter sources per thread in every chunk; chunks longer than a
-                    // tile are whole tiles
-                    const int kMinIter = 16;
-                    const int want = std::max(1, (kTargetCtas + ntile - 1) / ntile);
-                    const int most = std::max(1, nsrc / (kMinIter * lanes));
-                    const int nch = std::max(1, std::min(want, most));
-                    c = (nsrc + nch - 1) / nch;
-                    if (c > kTile) c = (c + kTile - 1) / kTile * kTile;
+                    // chunks of 2 to 4 source tiles, fewer when the launch already has enough
+                    // CTAs; no CTA's gravity then runs much longer than the others'
+                    const int want = std::max(1, kTargetCtas / std::max(1, tiles_all));
+                    const int c = (nsrc + want - 1) / want;
+                    chunk = std::min(std::max((c + kTile / 2) / kTile * kTile, 2 * kTile), 4 * kTile);
                 }
-                chunk = std::max(c, 1);
+                // the reducing CTA reads at most 2 batches of records per thread
+                const int nel = 3 * nsink;
+                const int max_chunks = 2 * kBatchRecords * std::max(1, kTile / nel);
+                if ((nsrc + chunk - 1) / chunk > max_chunks)
+                    chunk = ((nsrc + max_chunks - 1) / max_chunks + kTile - 1) / kTile * kTile;
+                chunk = std::max(chunk, 1);
             }
             const int nchunk = std::max(1, (nsrc + chunk - 1) / chunk);
             GravItem g;
@@ -525,7 +558,14 @@ void red_sim::build_plan()
         si.n_SI = (int)h.n_SI();
         si.n_massive = (int)h.n_massive();
         si.n_err = cfg.error_check_for_tp ? si.n : si.n_massive;
-        plan_gravity_items(si, (int)s, mode, chunk_override, lanes_cap, items, part, tiles);
+    }
+    int tiles_all = 0;
+    for (uint32_t s = 0; s < n_sys; s++) tiles_all += count_sink_tiles(sinfo[s], mode, lanes_cap);
+    for (uint32_t s = 0; s < n_sys; s++) {
+        const SysHost& h = sh[s];
+        SysInfo& si = sinfo[s];
+        (void)h;
+        plan_gravity_items(si, (int)s, mode, chunk_override, lanes_cap, tiles_all, items, part, tiles);
         for (int b = 0; b < si.n; b += kSegment) segs.push_back(Segment{(int)s, si.off + b, si.off + std::min(si.n, b + kSegment), 0});
         for (int b = 0; b < si.n; b += kFinishBodies)
             fsegs.push_back(Segment{(int)s, si.off + b, si.off + std::min(si.n, b + kFinishBodies), 0});
@@ -549,7 +589,7 @@ void red_sim::build_plan()
             // by more than one cell
             const double h = 2.0 * factor * rmax * (1.0 + 1.0e-6) + 1.0e-300;
             size_t m = 1024;
-            while (m < 2 * (size_t)n_small) m <<= 1;
+            while (m < 4 * (size_t)n_small) m <<= 1;
             g.inv_h = 1.0 / h;
             g.toff = (int)table;
             g.mask = (int)(m - 1);
@@ -642,7 +682,8 @@ StageParams red_sim::stage_params(int s, bool standalone)
 
 void red_sim::prep_positions()
 {
-    launch_prep(d_segs, (int)segs.size(), d_sinfo, d_sys, y_r, mass, radius, id, pos_hi[0], pos_lo[0], 1, stream);
+    launch_prep(d_segs, (int)segs.size(), d_sinfo, d_sys, y_r, mass, radius, id, pos_hi[0], pos_lo[0], pos_hi[1],
+                pos_lo[1], 1, stream);
     CK(cudaGetLastError());
     launches++;
 }

@@ -23,8 +23,7 @@
 
 namespace redgb {
 
-constexpr int kStarBatch = 4;   // star factors formed per pass of the epilogue
-constexpr int kBatch = 16;      // partial records loaded per batch by the reducing CTA
+constexpr int kStarBatch = 4;   // stars staged in shared memory (more are read from global memory)
 
 struct SmemStage {
     union {
@@ -33,7 +32,12 @@ struct SmemStage {
     } src;
     double acc[3 * kTile];          // per (sink, component) gravity sums
     double sc[kTile][3];            // drag factor and gas velocity per sink
-    double fs[kTile][kStarBatch];   // star factors per sink
+    float4 star_hi[kStarBatch], star_lo[kStarBatch];   // the stars' double-single positions
+    float2 star_m[kStarBatch];      // the stars' masses, double-single (0 for inactive stars)
+    union {                         // the tile's sinks (cp.async in the prologue)
+        struct { float4 hi[32]; float4 lo[32]; } f;
+        double d[3 * 32];
+    } snk;
     int flag;
 };
 
@@ -63,18 +67,35 @@ __device__ __forceinline__ double group_sum(double v, int lanes)
     return v;
 }
 
+// Double-single sum of the float2 partial records [c0, c1) of one element (FP32
+// modes), in order, loads issued in one batch per kBatchRecords records.
+__device__ __forceinline__ float2 sum_records_ds(const float2* base, long long stride, int c0, int c1)
+{
+    float2 a = make_float2(0.f, 0.f);
+    for (int b = c0; b < c1; b += kBatchRecords) {
+        float2 pv[kBatchRecords];
+#pragma unroll
+        for (int u = 0; u < kBatchRecords; u++) pv[u] = (b + u < c1) ? __ldcg(base + (b + u) * stride) : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < kBatchRecords; u++)
+            if (b + u < c1) a = dsn_add(a, pv[u]);
+    }
+    return a;
+}
+
 // Sum of the partial records [c0, c1) of one element (3 doubles per sink record,
 // element t of the tile at offset t), in order, loads issued in one batch per
-// kBatch records.
+// kBatchRecords records.
 __device__ __forceinline__ double sum_records(const double* base, long long stride, int c0, int c1)
 {
     double a = 0.0;
-    for (int b = c0; b < c1; b += kBatch) {
-        double pv[kBatch];
+    for (int b = c0; b < c1; b += kBatchRecords) {
+        double pv[kBatchRecords];
 #pragma unroll
-        for (int u = 0; u < kBatch; u++) pv[u] = (b + u < c1) ? __ldcg(base + (b + u) * stride) : 0.0;
+        for (int u = 0; u < kBatchRecords; u++) pv[u] = (b + u < c1) ? __ldcg(base + (b + u) * stride) : 0.0;
 #pragma unroll
-        for (int u = 0; u < kBatch; u++) a += pv[u];
+        for (int u = 0; u < kBatchRecords; u++)
+            if (b + u < c1) a += pv[u];
     }
     return a;
 }
@@ -87,8 +108,18 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src)
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
 }
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+// Waits until at most the most recent group of the thread's copies is in flight.
+__device__ __forceinline__ void cp_async_wait_prior() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+// Release / acquire at GPU scope (the writes of the whole CTA are ordered
+// before it by the preceding barrier; fences are cumulative).
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;\n" ::: "memory"); }
 
 // Operands of the epilogue of variant V, staged in shared memory by cp.async
 // at the start of the kernel: slot [slot][t] belongs to element thread t.
@@ -100,7 +131,7 @@ __host__ __device__ constexpr int var_nk(int v)
 }
 template <int V> struct Ops {
     static constexpr int nk = var_nk(V);
-    static constexpr int VS = 0, YR = 1, YV = 2, M = 3, RAD = 4, KR = 5, KV = 5 + nk, N = 5 + 2 * nk;
+    static constexpr int VS = 0, YR = 1, YV = 2, KR = 3, KV = 3 + nk, N = 3 + 2 * nk;
 };
 // Stage index of operand q of variant V.
 template <int V> __device__ __forceinline__ int op_src(int q)
@@ -114,21 +145,22 @@ template <int V> __device__ __forceinline__ int op_src(int q)
 // Gravity of the chunk's sources on SPT sinks per thread, FP32 modes.  The
 // first tile is in shared memory; (th, tl) carry the prefetch of the next.
 // On return thread lane l < 3 SPT of its sink group holds component l % 3 of
-// sink slot (group * SPT + l / 3) in `mine`.
+// sink slot (group * SPT + l / 3) in `mine`, a double-single sum.
 template <int MODE, int SPT>
 __device__ __forceinline__ void gravity_f32(SmemStage& sm, const StageParams& P, const GravItem& it, float4& th,
-                                            float4& tl, double& mine, int& mine_k, bool& mine_ok)
+                                            float4& tl, float2& mine, int& mine_k, bool& mine_ok)
 {
     const int t = threadIdx.x;
-    const int L = it.lanes;
+    constexpr int LC = SPT == 2 ? 8 : 0;   // the planner pairs 2 sinks per thread with 8 lanes
+    const int L = LC ? LC : it.lanes;
     const int grp = t / L, lane = t % L;
     float4 H[SPT], Lo[SPT];
 #pragma unroll
     for (int q = 0; q < SPT; q++) {
         const int k = grp * SPT + q;
-        const int i = it.sink0 + (k < it.nsink ? k : 0);   // inactive slots shadow sink 0 (results unused)
-        H[q] = P.pos_hi_in[i];
-        Lo[q] = MODE == MODE_MIXED ? P.pos_lo_in[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int ks = k < it.nsink ? k : 0;   // inactive slots shadow sink 0 (results unused)
+        H[q] = sm.snk.f.hi[ks];
+        Lo[q] = MODE == MODE_MIXED ? sm.snk.f.lo[ks] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     float acc[SPT][6];
 #pragma unroll
@@ -145,8 +177,7 @@ __device__ __forceinline__ void gravity_f32(SmemStage& sm, const StageParams& P,
         float tx[SPT], ty[SPT], tz[SPT];
 #pragma unroll
         for (int q = 0; q < SPT; q++) tx[q] = ty[q] = tz[q] = 0.f;
-#pragma unroll 4
-        for (int jj = lane; jj < nj; jj += L) {
+        auto source = [&](int jj) {
             const float4 h = sm.src.f.hi[jj];
             float4 l = make_float4(0.f, 0.f, 0.f, 0.f);
             if (MODE == MODE_MIXED) l = sm.src.f.lo[jj];
@@ -170,6 +201,13 @@ __device__ __forceinline__ void gravity_f32(SmemStage& sm, const StageParams& P,
                 ty[q] = fmaf(sc, dy, ty[q]);
                 tz[q] = fmaf(sc, dz, tz[q]);
             }
+        };
+        if (LC && nj == kTile) {
+#pragma unroll 4
+            for (int u = 0; u < kTile / (LC ? LC : 1); u++) source(lane + u * L);
+        } else {
+#pragma unroll 4
+            for (int jj = lane; jj < nj; jj += L) source(jj);
         }
 #pragma unroll
         for (int q = 0; q < SPT; q++) {
@@ -205,7 +243,7 @@ __device__ __forceinline__ void gravity_f32(SmemStage& sm, const StageParams& P,
                 hh = acc[q][2 * c];
                 ll = acc[q][2 * c + 1];
             }
-    mine = (double)hh + (double)ll;
+    mine = dsn_norm(hh, ll);
     mine_k = grp * SPT + lane / 3;
     mine_ok = lane < 3 * SPT && mine_k < it.nsink;
 }
@@ -220,7 +258,8 @@ __device__ __forceinline__ void gravity_f64(SmemStage& sm, const StageParams& P,
     const int k = t / L, lane = t % L;
     const bool has = k < it.nsink;
     const int i = it.sink0 + (has ? k : 0);
-    const double xi = P.r_in[3 * i], yi = P.r_in[3 * i + 1], zi = P.r_in[3 * i + 2];
+    const int ks = has ? k : 0;
+    const double xi = sm.snk.d[3 * ks], yi = sm.snk.d[3 * ks + 1], zi = sm.snk.d[3 * ks + 2];
     double ax = 0.0, ay = 0.0, az = 0.0;
     for (int j0 = it.src0; j0 < it.src1; j0 += kTile) {
         const int nj = min(kTile, it.src1 - j0);
@@ -346,18 +385,26 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
     const int ie = it.sink0 + ke;
     const int x = 3 * ie + ce;
     const int idi = P.id[ie];
-    const double rc = P.r_in[x];
     const bool drag_on = P.gas.enabled && it.cls == CLS_NSI;
     const bool need_vs = drag_on || V != 0;
+    if (kF32) {
+        if (t < it.nsink) {
+            cp_async16(&sm.snk.f.hi[t], P.pos_hi_in + it.sink0 + t);
+            cp_async16(&sm.snk.f.lo[t], P.pos_lo_in + it.sink0 + t);
+        }
+        if (t < min(kStarBatch, it.nstar)) {
+            cp_async16(&sm.star_hi[t], P.pos_hi_in + it.soff + t);
+            cp_async16(&sm.star_lo[t], P.pos_lo_in + it.soff + t);
+        }
+    } else if (t < nel) {
+        cp_async8(&sm.snk.d[t], P.r_in + 3 * it.sink0 + t);
+    }
+    cp_async_commit();
     if (elem) {
         if (need_vs) cp_async8(&ops[O::VS][t], P.Kr[s] + x);
         if constexpr (V >= 1 && V <= 14) {
             cp_async8(&ops[O::YR][t], P.y_r + x);
             cp_async8(&ops[O::YV][t], P.y_v + x);
-            if (ce == 0) {
-                cp_async8(&ops[O::M][t], P.mass + ie);
-                cp_async8(&ops[O::RAD][t], P.radius + ie);
-            }
         }
 #pragma unroll
         for (int q = 0; q < O::nk; q++) {
@@ -368,8 +415,7 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
     }
     cp_async_commit();
 
-    // ---- drag factor and star factors: scalars per sink, thread t < nsink ----
-    const bool star_term = kF32 && it.nstar > 0;
+    // ---- drag factor: scalars per sink, thread t < nsink (FP64, red's gas formulas) ----
     double decr = 0.0;
     if (drag_on) {
         const double ts = P.standalone ? P.t_standalone
@@ -377,43 +423,25 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
         decr = gas_reduction_factor(P.gas, ts);
     }
     const bool drag_act = drag_on && !(1.0e-6 > decr);
-    const bool sink_thread = t < it.nsink;
-    const int ib = it.sink0 + (sink_thread ? t : 0);
-    double bx = 0.0, by = 0.0, bz = 0.0;
-    if (star_term || drag_act) {
-        bx = P.r_in[3 * ib];
-        by = P.r_in[3 * ib + 1];
-        bz = P.r_in[3 * ib + 2];
-    }
-    if (drag_act && sink_thread) {
+    if (drag_act && t < it.nsink) {
+        const int ib = it.sink0 + t;
         double f, gx, gy;
-        drag_factor(P.gas, decr, P.mass[it.soff], bx, by, bz, P.Kr[s][3 * ib], P.Kr[s][3 * ib + 1],
-                    P.Kr[s][3 * ib + 2], P.cd[ib], P.radius[ib], P.density[ib], f, gx, gy);
+        drag_factor(P.gas, decr, P.mass[it.soff], P.r_in[3 * ib], P.r_in[3 * ib + 1], P.r_in[3 * ib + 2],
+                    P.Kr[s][3 * ib], P.Kr[s][3 * ib + 1], P.Kr[s][3 * ib + 2], P.cd[ib], P.radius[ib], P.density[ib],
+                    f, gx, gy);
         sm.sc[t][0] = f;
         sm.sc[t][1] = gx;
         sm.sc[t][2] = gy;
     }
-    // central-star term in FP64: m_j d / |d|^3 with |d|^-1 from rsqrt, the factor
-    // per (sink, star) formed by one thread per sink
-    auto star_factors = [&](int b0, int nst) {
-        if (sink_thread) {
-#pragma unroll
-            for (int q = 0; q < kStarBatch; q++) {
-                if (q < nst) {
-                    const int j = it.soff + b0 + q;
-                    const double dx = P.r_in[3 * j] - bx, dy = P.r_in[3 * j + 1] - by, dz = P.r_in[3 * j + 2] - bz;
-                    const double w = fma(dz, dz, fma(dy, dy, dx * dx));
-                    const double ri = rsqrt(w);
-                    sm.fs[t][q] = (j == ib || P.id[j] < 0) ? 0.0 : P.mass[j] * (ri * ri) * ri;
-                }
-            }
-        }
-    };
-    double sp[kStarBatch];
+    // ---- the stars' masses for the central-star term (FP32 modes), double-single ----
+    const bool star_term = kF32 && it.nstar > 0;
     const int nst0 = star_term ? min(kStarBatch, it.nstar) : 0;
-#pragma unroll
-    for (int q = 0; q < kStarBatch; q++) sp[q] = q < nst0 ? P.r_in[3 * (it.soff + q) + ce] : 0.0;
-    if (star_term) star_factors(0, nst0);
+    if (t < nst0) {
+        const int j = it.soff + t;
+        const double m = P.id[j] < 0 ? 0.0 : P.mass[j];
+        const float mh = __double2float_rn(m);
+        sm.star_m[t] = make_float2(mh, __double2float_rn(m - (double)mh));
+    }
     if (kF32) {
         sm.src.f.hi[t] = th;
         if (MODE == MODE_MIXED) sm.src.f.lo[t] = tl;
@@ -421,28 +449,17 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
         sm.src.d.d[t] = td;
         sm.src.d.id[t] = tid;
     }
+    cp_async_wait_prior();   // the sinks and stars; the epilogue's operands may still be in flight
     __syncthreads();
-    double sc_sum = 0.0;
-    if (star_term) {
-#pragma unroll
-        for (int q = 0; q < kStarBatch; q++)
-            if (q < nst0) sc_sum = fma(sm.fs[ke][q], sp[q] - rc, sc_sum);
-        for (int b0 = kStarBatch; b0 < it.nstar; b0 += kStarBatch) {   // more than kStarBatch stars
-            const int nst = min(kStarBatch, it.nstar - b0);
-            __syncthreads();
-            star_factors(b0, nst);
-            __syncthreads();
-            for (int q = 0; q < nst; q++) sc_sum = fma(sm.fs[ke][q], P.r_in[3 * (it.soff + b0 + q) + ce] - rc, sc_sum);
-        }
-    }
 
     // ---- gravity of the chunk's sources ----
-    double mine;
+    float2 mine_ds = make_float2(0.f, 0.f);   // FP32 modes: double-single sums
+    double mine = 0.0;                        // FP64 modes
     int mine_k;
     bool mine_ok;
     if constexpr (kF32) {
-        if (it.spt == 2) gravity_f32<MODE, 2>(sm, P, it, th, tl, mine, mine_k, mine_ok);
-        else gravity_f32<MODE, 1>(sm, P, it, th, tl, mine, mine_k, mine_ok);
+        if (it.spt == 2) gravity_f32<MODE, 2>(sm, P, it, th, tl, mine_ds, mine_k, mine_ok);
+        else gravity_f32<MODE, 1>(sm, P, it, th, tl, mine_ds, mine_k, mine_ok);
     } else {
         gravity_f64<MODE>(sm, P, it, td, tid, mine, mine_k, mine_ok);
     }
@@ -450,49 +467,88 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
 
     // ---- source chunks of one sink tile -> the CTA that finishes last sums them,
     // every thread of it on a contiguous range of chunks, in a fixed order ----
-    double a = 0.0;
+    float2 g_ds = make_float2(0.f, 0.f);   // gravity of the element, FP32 modes
+    double a = 0.0;                         // gravity of the element, FP64 modes
+    float2* acc2 = reinterpret_cast<float2*>(sm.acc);
     if (it.nchunk > 1) {
         if (mine_ok) {
-            double* p = P.partial + 3 * ((long long)it.part_off + (long long)it.chunk * it.nsink) + 3 * mine_k + mine_c;
-            *p = mine;
+            const long long rec = 3 * ((long long)it.part_off + (long long)it.chunk * it.nsink) + 3 * mine_k + mine_c;
+            if (kF32) reinterpret_cast<float2*>(P.partial)[rec] = mine_ds;
+            else P.partial[rec] = mine;
         }
-        __threadfence();
         __syncthreads();
         if (t == 0) {
+            fence_acq_rel_gpu();   // release the CTA's partial record
             const unsigned prev = atomicAdd(&P.tile_cnt[it.tile], 1u);
-            sm.flag = (prev == (unsigned)(it.nchunk - 1));
+            const bool last = prev == (unsigned)(it.nchunk - 1);
+            if (last) fence_acq_rel_gpu();   // acquire the other chunks' records
+            sm.flag = last;
         }
         __syncthreads();
         if (!sm.flag) {        // uniform
             cp_async_wait_all();   // no copy may land in shared memory after the CTA has gone
             return;
         }
-        __threadfence();
         const int nsplit = kTile / nel;
         const int sp_i = t / nel;
         const int e = t - sp_i * nel;
-        double part = 0.0;
-        if (sp_i < nsplit) {
-            const int c0 = (int)((long long)sp_i * it.nchunk / nsplit);
-            const int c1 = (int)((long long)(sp_i + 1) * it.nchunk / nsplit);
-            part = sum_records(P.partial + 3 * (long long)it.part_off + e, 3LL * it.nsink, c0, c1);
+        const int c0 = sp_i < nsplit ? sp_i * it.nchunk / nsplit : 0;
+        const int c1 = sp_i < nsplit ? (sp_i + 1) * it.nchunk / nsplit : 0;
+        const long long base = 3 * (long long)it.part_off + e;
+        if (kF32) {
+            acc2[t] = sum_records_ds(reinterpret_cast<const float2*>(P.partial) + base, 3LL * it.nsink, c0, c1);
+        } else {
+            sm.acc[t] = sum_records(P.partial + base, 3LL * it.nsink, c0, c1);
         }
-        sm.acc[t] = part;
         __syncthreads();
-        if (elem)
-            for (int q = 0; q < nsplit; q++) a += sm.acc[q * nel + t];
+        if (elem) {
+            for (int q = 0; q < nsplit; q++) {
+                if (kF32) g_ds = dsn_add(g_ds, acc2[q * nel + t]);
+                else a += sm.acc[q * nel + t];
+            }
+        }
         if (t == 0) P.tile_cnt[it.tile] = 0u;
     } else {
-        if (mine_ok) sm.acc[3 * mine_k + mine_c] = mine;
+        if (mine_ok) {
+            if (kF32) acc2[3 * mine_k + mine_c] = mine_ds;
+            else sm.acc[3 * mine_k + mine_c] = mine;
+        }
         __syncthreads();
-        if (elem) a = sm.acc[t];
+        if (elem) {
+            if (kF32) g_ds = acc2[t];
+            else a = sm.acc[t];
+        }
     }
+
+    // ---- central-star term (FP32 modes), double-single: m_j d / |d|^3 per star,
+    // each element thread forming the factor of its own sink ----
+    if (star_term && elem) {
+        const float4 H = sm.snk.f.hi[ke], Lo = sm.snk.f.lo[ke];
+        auto star_one = [&](const float4& S, const float4& SL, float2 m) {
+            const float2 dx = dsn_sub(dsn(S.x, SL.x), dsn(H.x, Lo.x));
+            const float2 dy = dsn_sub(dsn(S.y, SL.y), dsn(H.y, Lo.y));
+            const float2 dz = dsn_sub(dsn(S.z, SL.z), dsn(H.z, Lo.z));
+            const float2 r2 = dsn_add(dsn_add(dsn_mul(dx, dx), dsn_mul(dy, dy)), dsn_mul(dz, dz));
+            const float2 ri = dsn_rsqrt(r2);
+            const float2 f = dsn_mul(m, dsn_mul(dsn_mul(ri, ri), ri));
+            g_ds = dsn_add(g_ds, dsn_mul(f, ce == 0 ? dx : (ce == 1 ? dy : dz)));
+        };
+        for (int q = 0; q < nst0; q++)
+            if (it.soff + q != ie) star_one(sm.star_hi[q], sm.star_lo[q], sm.star_m[q]);
+        for (int j = it.soff + kStarBatch; j < it.soff + it.nstar; j++) {   // more than kStarBatch stars
+            if (j == ie) continue;
+            const double m = P.id[j] < 0 ? 0.0 : P.mass[j];
+            const float mh = __double2float_rn(m);
+            star_one(P.pos_hi_in[j], P.pos_lo_in[j], make_float2(mh, __double2float_rn(m - (double)mh)));
+        }
+    }
+    if (kF32) a = dsn_to_double(g_ds);
+
     cp_async_wait_all();
     if (!elem) return;
 
     // ---- element-wise FP64 epilogue ----
     const double vs = need_vs ? ops[O::VS][t] : 0.0;   // stage velocity of the element
-    if (star_term) a = sc_sum + a;
     if (!(idi > 0)) a = 0.0;   // calc_grav_accel_naive zeroes inactive sinks (pp_disk.cu:386-388)
     if (drag_act) {
         const double g = ce == 0 ? sm.sc[ke][1] : (ce == 1 ? sm.sc[ke][2] : 0.0);
@@ -532,11 +588,7 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
         }
         P.r_out[x] = orr;
         P.Kr[P.next][x] = ovv;
-        write_pos_c(P.pos_hi_out, P.pos_lo_out, ie, ce, orr);
-        if (ce == 0) {
-            reinterpret_cast<float*>(P.pos_hi_out + ie)[3] = __double2float_rn(idi >= 0 ? ops[O::M][t] : 0.0);
-            reinterpret_cast<float*>(P.pos_lo_out + ie)[3] = __double2float_rn(ops[O::RAD][t]);
-        }
+        write_pos_c(P.pos_hi_out, P.pos_lo_out, ie, ce, orr);   // x, y, z; k_prep holds the .w words
     } else if constexpr (V == 15 || V == 16) {
         double e = 0.0;
         if (ie - it.soff < it.nerr) {
