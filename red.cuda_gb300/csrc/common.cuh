@@ -51,9 +51,15 @@ __device__ __forceinline__ void ds_merge(float& ah, float& al, float bh, float b
 }
 
 // Double-single numbers as float2 (x = hi, y = lo, hi + lo the value, |lo| <=
-// ulp(hi) after renormalisation): Dekker (1971) and Knuth's TwoSum, the
-// product's error term from fmaf.  About 48 significant bits.
+// ulp(hi)): Dekker (1971) and Knuth's TwoSum, the product's error term from
+// fmaf.  About 48 significant bits.
 __device__ __forceinline__ float2 dsn(float hi, float lo) { return make_float2(hi, lo); }
+// a + b with |a| >= |b| (Dekker's Fast2Sum)
+__device__ __forceinline__ float2 dsn_fast(float a, float b)
+{
+    const float s = a + b;
+    return make_float2(s, b - (s - a));
+}
 __device__ __forceinline__ float2 dsn_norm(float a, float b)
 {
     float s, e;
@@ -64,35 +70,70 @@ __device__ __forceinline__ float2 dsn_add(float2 a, float2 b)
 {
     float s, e;
     two_sum(a.x, b.x, s, e);
-    return dsn_norm(s, e + (a.y + b.y));
+    return dsn_fast(s, e + (a.y + b.y));
 }
-__device__ __forceinline__ float2 dsn_sub(float2 a, float2 b) { return dsn_add(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 dsn_sub(float2 a, float2 b)
+{
+    float s, e;
+    two_sum(a.x, -b.x, s, e);
+    return dsn_fast(s, e + (a.y - b.y));
+}
 __device__ __forceinline__ float2 dsn_mul(float2 a, float2 b)
 {
     const float p = a.x * b.x;
-    float e = fmaf(a.x, b.x, -p);
-    e = fmaf(a.x, b.y, fmaf(a.y, b.x, e));
-    return dsn_norm(p, e);
+    const float e = fmaf(a.x, b.y, fmaf(a.y, b.x, fmaf(a.x, b.x, -p)));
+    return dsn_fast(p, e);
 }
-// 1 / sqrt(x) for x > 0: the hardware estimate refined by two Newton steps
-// y <- y + y (1 - x y^2) / 2, the second in double-single arithmetic.
+__device__ __forceinline__ float2 dsn_sqr(float2 a)
+{
+    const float p = a.x * a.x;
+    return dsn_fast(p, fmaf(a.x + a.x, a.y, fmaf(a.x, a.x, -p)));
+}
+// 1 / sqrt(x) for x > 0: the hardware estimate, one FP32 Newton step (to
+// ~1 ulp of FP32), then one Newton step y + y (1 - x y^2) / 2 with the
+// residual formed in double-single: relative error ~2e-14.
 __device__ __forceinline__ float2 dsn_rsqrt(float2 x)
 {
-    const float y = rsqrtf(x.x);
-    const float2 t = dsn_mul(x, dsn_norm(y * y, fmaf(y, y, -(y * y))));
+    float y = rsqrtf(x.x);
+    y = y * fmaf(-0.5f * x.x, y * y, 1.5f);
+    const float yy = y * y;
+    const float2 t = dsn_mul(x, make_float2(yy, fmaf(y, y, -yy)));
     const float r = (1.0f - t.x) - t.y;
-    const float2 y1 = dsn_norm(y, 0.5f * y * r);
-    const float2 r1 = dsn_sub(make_float2(1.0f, 0.0f), dsn_mul(x, dsn_mul(y1, y1)));
-    const float2 c = dsn_mul(y1, r1);
-    return dsn_add(y1, make_float2(0.5f * c.x, 0.5f * c.y));
+    return dsn_fast(y, 0.5f * y * r);
 }
-__device__ __forceinline__ double dsn_to_double(float2 a) { return (double)a.x + (double)a.y; }
 
+// x -> (h, l), h + l = x to 2^-48 relative: h is x truncated to 24 significant
+// bits, l the remaining 29 bits rounded to 24.  Built from the bits with
+// integer operations (GB300's FP64 pipe runs at 1/64 of FP32); values outside
+// FP32's normal range (|x| < 2^-74 for l, zero, Inf, NaN) take the FP64 route.
 __device__ __forceinline__ void split_ds(double x, float& h, float& l)
 {
-    h = __double2float_rn(x);
-    l = __double2float_rn(x - (double)h);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e >= 1023 - 74 + 23 && e <= 1023 + 127) {
+        const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+        h = __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)((b >> 29) & 0x7FFFFFu));
+        const float m = __uint2float_rn((unsigned)(b & 0x1FFFFFFFull));        // the low 29 bits, rounded
+        const float scale = __uint_as_float((unsigned)(e - 1075 + 127) << 23);  // 2^(e - 1023 - 52)
+        l = __uint_as_float(__float_as_uint(m * scale) | sign);
+    } else {
+        h = __double2float_rn(x);
+        l = __double2float_rn(x - (double)h);
+    }
 }
+
+// Exact float -> double from the bits (zero and FP32 denormals give signed
+// zero; Inf and NaN are kept).
+__device__ __forceinline__ double f2d_bits(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xFFu;
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    if (e == 0) return __longlong_as_double((long long)sign);
+    const unsigned long long ee = e == 0xFFu ? 0x7FFull : (unsigned long long)(e + 896u);
+    return __longlong_as_double((long long)(sign | (ee << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
+__device__ __forceinline__ double dsn_to_double(float2 a) { return f2d_bits(a.x) + f2d_bits(a.y); }
 
 __device__ __forceinline__ void write_pos(float4* hi, float4* lo, int i, double x, double y, double z,
                                           double m_eff, double radius)

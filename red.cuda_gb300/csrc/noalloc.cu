@@ -23,7 +23,7 @@
 #include <mutex>
 #include <vector>
 
-#include "redgb_dev.cuh"
+#include "common.cuh"
 #include "redgb.h"
 
 using namespace redgb;
@@ -53,18 +53,9 @@ __global__ void k_noalloc_prep(int n, const double* r, const double* mass, const
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float4 H, L;
-    const double x = r[3 * i], y = r[3 * i + 1], z = r[3 * i + 2];
-    H.x = __double2float_rn(x);
-    H.y = __double2float_rn(y);
-    H.z = __double2float_rn(z);
-    L.x = __double2float_rn(x - (double)H.x);
-    L.y = __double2float_rn(y - (double)H.y);
-    L.z = __double2float_rn(z - (double)H.z);
-    H.w = __double2float_rn(id[i] >= 0 ? mass[i] : 0.0);
-    L.w = radius ? __double2float_rn(radius[i]) : 0.f;
-    hi[i] = H;
-    lo[i] = L;
+    // the same double-single split as the allocating path (k_prep)
+    redgb::write_pos(hi, lo, i, r[3 * i], r[3 * i + 1], r[3 * i + 2], id[i] >= 0 ? mass[i] : 0.0,
+                     radius ? radius[i] : 0.0);
 }
 
 }  // namespace
@@ -104,7 +95,7 @@ extern "C" int red_calc_accel_noalloc(const red_accel_args_t* a)
     std::vector<GravItem> items;
     size_t part = 0;
     int tiles = 0;
-    plan_gravity_items(si, 0, a->precision, 0, 32, count_sink_tiles(si, a->precision, 32), items, part, tiles);
+    plan_gravity_items(si, 0, a->precision, 0, 32, count_sink_tiles(si, a->precision, 32), nullptr, items, part, tiles);
     const size_t off_part = ((kOffPos + 2 * pos_bytes + 255) / 256) * 256;
     if (items.size() > kMaxItems || (size_t)tiles > kMaxTiles || off_part + part * 3 * sizeof(double) > kScratchBytes)
         return fail(RED_ERR_ARG, "red_calc_accel_noalloc: the launch plan does not fit the scratch array");

@@ -73,6 +73,8 @@ struct GravItem {
     int nstar;
     int nerr;             // bodies [soff, soff + nerr) enter the error norm
     int spt;              // sinks per thread group (1, or 2 in the FP32 modes: lanes >= 8)
+    int mstar_set;        // 1: mstar holds the mass of the system's first star (0 if inactive)
+    float mstar_hi, mstar_lo;   // that mass, double-single
     int pad[2];
 };
 
@@ -225,8 +227,10 @@ struct EjhcParams {
 // tiles_all: sink tiles of every system planned into the same launch (count_sink_tiles).
 constexpr int kBatchRecords = 16;   // partial records loaded per batch by the reducing CTA
 int count_sink_tiles(const SysInfo& si, int mode, int lanes_cap);
+// star_mass: the effective mass of the system's first star (0 if its id < 0), or
+// nullptr when the host does not hold it (the kernel then reads it).
 void plan_gravity_items(const SysInfo& si, int sys, int mode, int chunk_override, int lanes_cap, int tiles_all,
-                        std::vector<GravItem>& items, size_t& part, int& tiles);
+                        const double* star_mass, std::vector<GravItem>& items, size_t& part, int& tiles);
 
 // Host-side launchers (kernels.cu, stage_*.cu).  The stage kernel's mode
 // fixes the arithmetic of the stage combinations: FP64_EXACT combines in red's

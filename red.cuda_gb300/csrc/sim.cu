@@ -192,7 +192,7 @@ int count_sink_tiles(const SysInfo& si, int mode, int lanes_cap)
 }
 
 void plan_gravity_items(const SysInfo& si, int s, int mode, int chunk_override, int lanes_cap, int tiles_all,
-                        std::vector<GravItem>& items, size_t& part, int& tiles)
+                        const double* star_mass, std::vector<GravItem>& items, size_t& part, int& tiles)
 {
     // the launch should hold several waves of CTAs (6 resident on each of
     // GB300's 152 SMs); tiles_all counts the sink tiles of every system in it
@@ -241,6 +241,11 @@ void plan_gravity_items(const SysInfo& si, int s, int mode, int chunk_override, 
             g.soff = si.off;
             g.nstar = si.n_star;
             g.nerr = si.n_err;
+            if (star_mass && si.n_star > 0) {
+                g.mstar_set = 1;
+                g.mstar_hi = (float)*star_mass;
+                g.mstar_lo = (float)(*star_mass - (double)g.mstar_hi);
+            }
             g.tile = nchunk > 1 ? tiles++ : -1;
             g.part_off = (int)part;
             if (nchunk > 1) part += (size_t)nchunk * nsink;
@@ -311,6 +316,7 @@ struct red_sim {
     void ensure_xfer(size_t bytes);
     void pack_to_host(uint32_t s);
     std::vector<double> grid_rmax;   // largest small-body radius the collision grid was planned for
+    std::vector<double> star_mass;   // the first star's effective mass the plan was made with
 
     // plan
     std::vector<GravItem> items;
@@ -545,8 +551,12 @@ void red_sim::build_plan()
     grid_rmax.assign(n_sys, 0.0);
     size_t table = 0;
     // radii, for the cell size of the collision grid
-    std::vector<double> h_radius(n_cap);
+    std::vector<double> h_radius(n_cap), h_mass(n_cap);
+    std::vector<int> h_id(n_cap);
     CK(cudaMemcpy(h_radius.data(), radius, n_cap * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(h_mass.data(), mass, n_cap * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(h_id.data(), id, n_cap * sizeof(int), cudaMemcpyDeviceToHost));
+    star_mass.assign(n_sys, 0.0);
     size_t part = 0;
     int tiles = 0;
     for (uint32_t s = 0; s < n_sys; s++) {
@@ -565,7 +575,8 @@ void red_sim::build_plan()
         const SysHost& h = sh[s];
         SysInfo& si = sinfo[s];
         (void)h;
-        plan_gravity_items(si, (int)s, mode, chunk_override, lanes_cap, tiles_all, items, part, tiles);
+        star_mass[s] = si.n_star > 0 && h_id[si.off] >= 0 ? h_mass[si.off] : 0.0;
+        plan_gravity_items(si, (int)s, mode, chunk_override, lanes_cap, tiles_all, &star_mass[s], items, part, tiles);
         for (int b = 0; b < si.n; b += kSegment) segs.push_back(Segment{(int)s, si.off + b, si.off + std::min(si.n, b + kSegment), 0});
         for (int b = 0; b < si.n; b += kFinishBodies)
             fsegs.push_back(Segment{(int)s, si.off + b, si.off + std::min(si.n, b + kFinishBodies), 0});
@@ -1513,11 +1524,14 @@ int red_set_state(red_sim* sim, uint32_t sys, const red_var4_t* r, const red_var
     sim->launches++;
     bool replan = false;
     if (p) {
-        // the collision grid's cells must stay wider than the largest collision distance
+        // the collision grid's cells must stay wider than the largest collision distance,
+        // and the work items carry the first star's mass
         double rmax = 0.0;
         for (size_t k = h.n_SI(); k < n; k++) rmax = std::max(rmax, p[k].radius);
         replan = rmax > sim->grid_rmax[sys];
+        if (h.playing[0] > 0 && p[0].mass != sim->star_mass[sys]) replan = true;
     }
+    if (md) replan = true;   // ids decide which bodies act as sources
     if (replan) {
         CK(cudaStreamSynchronize(sim->stream));
         sim->build_plan();

@@ -437,10 +437,14 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
     const bool star_term = kF32 && it.nstar > 0;
     const int nst0 = star_term ? min(kStarBatch, it.nstar) : 0;
     if (t < nst0) {
-        const int j = it.soff + t;
-        const double m = P.id[j] < 0 ? 0.0 : P.mass[j];
-        const float mh = __double2float_rn(m);
-        sm.star_m[t] = make_float2(mh, __double2float_rn(m - (double)mh));
+        if (t == 0 && it.mstar_set) {
+            sm.star_m[0] = make_float2(it.mstar_hi, it.mstar_lo);
+        } else {
+            const int j = it.soff + t;
+            const double m = P.id[j] < 0 ? 0.0 : P.mass[j];
+            const float mh = __double2float_rn(m);
+            sm.star_m[t] = make_float2(mh, __double2float_rn(m - (double)mh));
+        }
     }
     if (kF32) {
         sm.src.f.hi[t] = th;
@@ -524,13 +528,13 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
     // each element thread forming the factor of its own sink ----
     if (star_term && elem) {
         const float4 H = sm.snk.f.hi[ke], Lo = sm.snk.f.lo[ke];
-        auto star_one = [&](const float4& S, const float4& SL, float2 m) {
+        auto star_one = [&](float4 S, float4 SL, float2 m) {
             const float2 dx = dsn_sub(dsn(S.x, SL.x), dsn(H.x, Lo.x));
             const float2 dy = dsn_sub(dsn(S.y, SL.y), dsn(H.y, Lo.y));
             const float2 dz = dsn_sub(dsn(S.z, SL.z), dsn(H.z, Lo.z));
-            const float2 r2 = dsn_add(dsn_add(dsn_mul(dx, dx), dsn_mul(dy, dy)), dsn_mul(dz, dz));
+            const float2 r2 = dsn_add(dsn_add(dsn_sqr(dx), dsn_sqr(dy)), dsn_sqr(dz));
             const float2 ri = dsn_rsqrt(r2);
-            const float2 f = dsn_mul(m, dsn_mul(dsn_mul(ri, ri), ri));
+            const float2 f = dsn_mul(m, dsn_mul(dsn_sqr(ri), ri));
             g_ds = dsn_add(g_ds, dsn_mul(f, ce == 0 ? dx : (ce == 1 ? dy : dz)));
         };
         for (int q = 0; q < nst0; q++)
