@@ -95,7 +95,9 @@ extern "C" int red_calc_accel_noalloc(const red_accel_args_t* a)
     std::vector<GravItem> items;
     size_t part = 0;
     int tiles = 0;
-    plan_gravity_items(si, 0, a->precision, 0, 32, count_sink_tiles(si, a->precision, 32), nullptr, items, part, tiles);
+    long long short_ctas = 0;
+    const int tiles_all = count_sink_tiles(si, a->precision, 32, &short_ctas);
+    plan_gravity_items(si, 0, a->precision, 0, 32, tiles_all, short_ctas <= 6 * 152, nullptr, items, part, tiles);
     const size_t off_part = ((kOffPos + 2 * pos_bytes + 255) / 256) * 256;
     if (items.size() > kMaxItems || (size_t)tiles > kMaxTiles || off_part + part * 3 * sizeof(double) > kScratchBytes)
         return fail(RED_ERR_ARG, "red_calc_accel_noalloc: the launch plan does not fit the scratch array");

@@ -226,11 +226,14 @@ struct EjhcParams {
 // Host-side plan of the stage kernel for one system (sim.cu).
 // tiles_all: sink tiles of every system planned into the same launch (count_sink_tiles).
 constexpr int kBatchRecords = 16;   // partial records loaded per batch by the reducing CTA
-int count_sink_tiles(const SysInfo& si, int mode, int lanes_cap);
+// short_ctas (optional) accumulates the CTAs the system would need with chunks of
+// two source tiles; short_chunks selects those chunks for the plan.
+int count_sink_tiles(const SysInfo& si, int mode, int lanes_cap, long long* short_ctas);
 // star_mass: the effective mass of the system's first star (0 if its id < 0), or
 // nullptr when the host does not hold it (the kernel then reads it).
 void plan_gravity_items(const SysInfo& si, int sys, int mode, int chunk_override, int lanes_cap, int tiles_all,
-                        const double* star_mass, std::vector<GravItem>& items, size_t& part, int& tiles);
+                        bool short_chunks, const double* star_mass, std::vector<GravItem>& items, size_t& part,
+                        int& tiles);
 
 // Host-side launchers (kernels.cu, stage_*.cu).  The stage kernel's mode
 // fixes the arithmetic of the stage combinations: FP64_EXACT combines in red's

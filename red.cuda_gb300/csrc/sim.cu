@@ -175,7 +175,7 @@ static void class_shape(int mode, int nsink_all, int nsrc, int lanes_cap, int& l
     while (lanes < 32 && lanes < lanes_cap && (2 * lanes * nsink_all <= kTile || 256 * 2 * lanes <= nsrc)) lanes *= 2;
 }
 
-int count_sink_tiles(const SysInfo& si, int mode, int lanes_cap)
+int count_sink_tiles(const SysInfo& si, int mode, int lanes_cap, long long* short_ctas)
 {
     GravClass cls[3];
     gravity_classes(si, mode, cls);
@@ -183,19 +183,26 @@ int count_sink_tiles(const SysInfo& si, int mode, int lanes_cap)
     for (const GravClass& q : cls) {
         const int nsink_all = q.s1 - q.s0;
         if (nsink_all <= 0) continue;
+        const int nsrc = std::max(0, q.j1 - q.j0);
         int lanes, spt;
-        class_shape(mode, nsink_all, std::max(0, q.j1 - q.j0), lanes_cap, lanes, spt);
+        class_shape(mode, nsink_all, nsrc, lanes_cap, lanes, spt);
         const int tile_sinks = kTile / lanes * spt;
-        n += (nsink_all + tile_sinks - 1) / tile_sinks;
+        const int nt = (nsink_all + tile_sinks - 1) / tile_sinks;
+        n += nt;
+        if (short_ctas) *short_ctas += (long long)nt * std::max(1, (nsrc + 2 * kTile - 1) / (2 * kTile));
     }
     return n;
 }
 
 void plan_gravity_items(const SysInfo& si, int s, int mode, int chunk_override, int lanes_cap, int tiles_all,
-                        const double* star_mass, std::vector<GravItem>& items, size_t& part, int& tiles)
+                        bool short_chunks, const double* star_mass, std::vector<GravItem>& items, size_t& part,
+                        int& tiles)
 {
-    // the launch should hold several waves of CTAs (6 resident on each of
-    // GB300's 152 SMs); tiles_all counts the sink tiles of every system in it
+    // Two regimes.  When chunks of two source tiles keep the whole launch within
+    // one wave (short_chunks), every chunk is two tiles, staged in shared memory
+    // at once: the launch is as short as its slowest CTA.  Otherwise the launch
+    // should hold several waves of CTAs (6 resident on each of GB300's 152 SMs);
+    // tiles_all counts the sink tiles of every system in it.
     const int kTargetCtas = 8 * 6 * 152;
     GravClass cls[3];
     gravity_classes(si, mode, cls);
@@ -219,7 +226,8 @@ void plan_gravity_items(const SysInfo& si, int s, int mode, int chunk_override, 
                     // CTAs; no CTA's gravity then runs much longer than the others'
                     const int want = std::max(1, kTargetCtas / std::max(1, tiles_all));
                     const int c = (nsrc + want - 1) / want;
-                    chunk = std::min(std::max((c + kTile / 2) / kTile * kTile, 2 * kTile), 4 * kTile);
+                    chunk = short_chunks ? 2 * kTile
+                                         : std::min(std::max((c + kTile / 2) / kTile * kTile, 2 * kTile), 16 * kTile);
                 }
                 // the reducing CTA reads at most 2 batches of records per thread
                 const int nel = 3 * nsink;
@@ -570,13 +578,16 @@ void red_sim::build_plan()
         si.n_err = cfg.error_check_for_tp ? si.n : si.n_massive;
     }
     int tiles_all = 0;
-    for (uint32_t s = 0; s < n_sys; s++) tiles_all += count_sink_tiles(sinfo[s], mode, lanes_cap);
+    long long short_ctas = 0;
+    for (uint32_t s = 0; s < n_sys; s++) tiles_all += count_sink_tiles(sinfo[s], mode, lanes_cap, &short_ctas);
+    const bool short_chunks = short_ctas <= 6 * 152;   // one wave at 6 CTAs per SM
     for (uint32_t s = 0; s < n_sys; s++) {
         const SysHost& h = sh[s];
         SysInfo& si = sinfo[s];
         (void)h;
         star_mass[s] = si.n_star > 0 && h_id[si.off] >= 0 ? h_mass[si.off] : 0.0;
-        plan_gravity_items(si, (int)s, mode, chunk_override, lanes_cap, tiles_all, &star_mass[s], items, part, tiles);
+        plan_gravity_items(si, (int)s, mode, chunk_override, lanes_cap, tiles_all, short_chunks, &star_mass[s], items,
+                           part, tiles);
         for (int b = 0; b < si.n; b += kSegment) segs.push_back(Segment{(int)s, si.off + b, si.off + std::min(si.n, b + kSegment), 0});
         for (int b = 0; b < si.n; b += kFinishBodies)
             fsegs.push_back(Segment{(int)s, si.off + b, si.off + std::min(si.n, b + kFinishBodies), 0});

@@ -27,7 +27,7 @@ constexpr int kStarBatch = 4;   // stars staged in shared memory (more are read 
 
 struct SmemStage {
     union {
-        struct { float4 hi[kTile]; float4 lo[kTile]; } f;
+        struct { float4 hi[2 * kTile]; float4 lo[2 * kTile]; } f;   // up to two tiles staged at once
         struct { D4 d[kTile]; int id[kTile]; } d;
     } src;
     double acc[3 * kTile];          // per (sink, component) gravity sums
@@ -147,8 +147,8 @@ template <int V> __device__ __forceinline__ int op_src(int q)
 // On return thread lane l < 3 SPT of its sink group holds component l % 3 of
 // sink slot (group * SPT + l / 3) in `mine`, a double-single sum.
 template <int MODE, int SPT>
-__device__ __forceinline__ void gravity_f32(SmemStage& sm, const StageParams& P, const GravItem& it, float4& th,
-                                            float4& tl, float2& mine, int& mine_k, bool& mine_ok)
+__device__ __forceinline__ void gravity_f32(SmemStage& sm, const StageParams& P, const GravItem& it, bool staged,
+                                            float4& th, float4& tl, float2& mine, int& mine_k, bool& mine_ok)
 {
     const int t = threadIdx.x;
     constexpr int LC = SPT == 2 ? 8 : 0;   // the planner pairs 2 sinks per thread with 8 lanes
@@ -169,7 +169,8 @@ __device__ __forceinline__ void gravity_f32(SmemStage& sm, const StageParams& P,
         for (int c = 0; c < 6; c++) acc[q][c] = 0.f;
     for (int j0 = it.src0; j0 < it.src1; j0 += kTile) {
         const int nj = min(kTile, it.src1 - j0);
-        const bool more = j0 + kTile < it.src1;
+        const bool more = !staged && j0 + kTile < it.src1;
+        const int base = staged ? j0 - it.src0 : 0;   // staged chunks hold all their tiles
         if (more && t < min(kTile, it.src1 - j0 - kTile)) {
             th = P.pos_hi_in[j0 + kTile + t];
             if (MODE == MODE_MIXED) tl = P.pos_lo_in[j0 + kTile + t];
@@ -178,9 +179,9 @@ __device__ __forceinline__ void gravity_f32(SmemStage& sm, const StageParams& P,
 #pragma unroll
         for (int q = 0; q < SPT; q++) tx[q] = ty[q] = tz[q] = 0.f;
         auto source = [&](int jj) {
-            const float4 h = sm.src.f.hi[jj];
+            const float4 h = sm.src.f.hi[base + jj];
             float4 l = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (MODE == MODE_MIXED) l = sm.src.f.lo[jj];
+            if (MODE == MODE_MIXED) l = sm.src.f.lo[base + jj];
 #pragma unroll
             for (int q = 0; q < SPT; q++) {
                 float dx, dy, dz;
@@ -365,11 +366,15 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
     float4 th = make_float4(0.f, 0.f, 0.f, 0.f), tl = th;
     D4 td{0.0, 0.0, 0.0, 0.0};
     int tid = 0;
+    // FP32 modes: chunks of up to two tiles go to shared memory by cp.async at once
+    const bool staged = kF32 && it.src1 - it.src0 <= 2 * kTile;
     if (t < min(kTile, it.src1 - it.src0)) {
         const int j = it.src0 + t;
         if (kF32) {
-            th = P.pos_hi_in[j];
-            if (MODE == MODE_MIXED) tl = P.pos_lo_in[j];
+            if (!staged) {
+                th = P.pos_hi_in[j];
+                if (MODE == MODE_MIXED) tl = P.pos_lo_in[j];
+            }
         } else {
             tid = P.id[j];
             const double m = P.mass[j];
@@ -395,6 +400,12 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
         if (t < min(kStarBatch, it.nstar)) {
             cp_async16(&sm.star_hi[t], P.pos_hi_in + it.soff + t);
             cp_async16(&sm.star_lo[t], P.pos_lo_in + it.soff + t);
+        }
+        if (staged) {
+            for (int k = t; k < it.src1 - it.src0; k += kTile) {
+                cp_async16(&sm.src.f.hi[k], P.pos_hi_in + it.src0 + k);
+                if (MODE == MODE_MIXED) cp_async16(&sm.src.f.lo[k], P.pos_lo_in + it.src0 + k);
+            }
         }
     } else if (t < nel) {
         cp_async8(&sm.snk.d[t], P.r_in + 3 * it.sink0 + t);
@@ -447,8 +458,10 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
         }
     }
     if (kF32) {
-        sm.src.f.hi[t] = th;
-        if (MODE == MODE_MIXED) sm.src.f.lo[t] = tl;
+        if (!staged) {
+            sm.src.f.hi[t] = th;
+            if (MODE == MODE_MIXED) sm.src.f.lo[t] = tl;
+        }
     } else {
         sm.src.d.d[t] = td;
         sm.src.d.id[t] = tid;
@@ -462,8 +475,8 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
     int mine_k;
     bool mine_ok;
     if constexpr (kF32) {
-        if (it.spt == 2) gravity_f32<MODE, 2>(sm, P, it, th, tl, mine_ds, mine_k, mine_ok);
-        else gravity_f32<MODE, 1>(sm, P, it, th, tl, mine_ds, mine_k, mine_ok);
+        if (it.spt == 2) gravity_f32<MODE, 2>(sm, P, it, staged, th, tl, mine_ds, mine_k, mine_ok);
+        else gravity_f32<MODE, 1>(sm, P, it, staged, th, tl, mine_ds, mine_k, mine_ok);
     } else {
         gravity_f64<MODE>(sm, P, it, td, tid, mine, mine_k, mine_ok);
     }
