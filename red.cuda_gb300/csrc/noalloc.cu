@@ -34,7 +34,7 @@ constexpr size_t kScratchBytes = 4u << 20;          // 4 MiB
 constexpr size_t kMaxItems = 8192;                   // stage-kernel CTAs
 constexpr size_t kMaxTiles = 4096;                   // chunked sink tiles
 
-__device__ __align__(256) unsigned char g_scratch[kScratchBytes];
+static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
