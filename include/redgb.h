@@ -231,6 +231,45 @@ typedef struct {
 } red_accel_args_t;
 int red_calc_accel_noalloc(const red_accel_args_t* args);
 
+/* ---- Learned step proposer ---------------------------------------------
+ * A BF16 MLP (12 -> 64 -> 64 -> 1, SiLU, FP32 accumulation) proposes each
+ * system's next step from features of its accepted state (log|dt|, log of
+ * the error / tol, log of the smallest protoplanet-body distance in Hill
+ * radii, log max|a|, max |v|/v_kep, log N, mean / rms / max of e and i).  The
+ * embedded error estimate judges every try as before; a rejected proposal is
+ * retried with the classical controller's step (int_rungekutta8.cu:690-716).
+ * red.cuda has no learned component: these entry points have no counterpart
+ * in the reference.  Parameters are flat: W1[64][12], b1[64], W2[64][64],
+ * b2[64], w3[64], b3. */
+#define RED_MLP_NFEAT 12
+typedef struct {
+    float x_mean[RED_MLP_NFEAT], x_std[RED_MLP_NFEAT];   /* feature normalisation */
+    float y_mean, y_std;                                  /* of the target log|dt| */
+} red_mlp_norm_t;
+uint32_t red_mlp_param_count(void);
+/* Device buffers: w_bf16 (param_count BF16), x (n x 12 raw features) -> out
+ * (n predicted log|dt|). */
+int red_mlp_predict(const void* w_bf16, const red_mlp_norm_t* norm, const float* x, float* out, uint32_t n,
+                    void* stream);
+/* Gradient of sum_r (y_r - t_r)^2 / (2 n) over n rows of normalised features xn
+ * (n x 12) and targets tn, into grad (param_count floats) and loss (1 float);
+ * device buffers, deterministic (fixed-order reduction). */
+int red_mlp_grad(const void* w_bf16, const float* xn, const float* tn, uint32_t n, float* grad, float* loss,
+                 void* stream);
+/* One Adam step on FP32 master weights (device); refreshes the BF16 copy. */
+int red_mlp_adam(float* master, void* w_bf16, float* m, float* v, const float* grad, uint32_t step, float lr,
+                 float beta1, float beta2, float eps, void* stream);
+/* Enables the proposals (host copy of the BF16 weights).  The proposed step is
+ * safety * exp(prediction), its ratio to the last accepted step clamped to
+ * [ratio_lo, ratio_hi], then to the output interval.  Adaptive runs only. */
+int red_set_step_proposer(red_sim* sim, const uint16_t* w_bf16, const red_mlp_norm_t* norm, double safety,
+                          double ratio_lo, double ratio_hi);
+int red_clear_step_proposer(red_sim* sim);
+/* Logs (features of an accepted state, log|dt| of the next accepted step)
+ * records, 13 floats each, into a device buffer of `capacity` records (0 stops). */
+int red_log_features(red_sim* sim, uint32_t capacity);
+int red_get_feature_log(red_sim* sim, float* out, uint32_t cap, uint32_t* n_out, int32_t reset);
+
 const char* red_last_error(void);
 const char* red_version(void);
 

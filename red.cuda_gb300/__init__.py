@@ -7,6 +7,6 @@ package is a thin ctypes mirror of that ABI (lib.py) plus host utilities:
 red's record types (types.py), file formats (redio.py) and synthetic disks
 (ic.py).
 """
-from . import types, redio, ic, shard  # noqa: F401
+from . import types, redio, ic, shard, proposer  # noqa: F401
 from .build import build  # noqa: F401
 from .lib import Sim, RedError, load, EXPORTS  # noqa: F401

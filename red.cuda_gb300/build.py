@@ -19,7 +19,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
-UNITS = ["stage_mixed.cu", "stage_fp64.cu", "stage_exact.cu", "stage_fp32.cu", "kernels.cu", "sim.cu", "noalloc.cu"]
+UNITS = ["stage_mixed.cu", "stage_fp64.cu", "stage_exact.cu", "stage_fp32.cu", "kernels.cu", "sim.cu", "noalloc.cu",
+         "proposer.cu"]
 # The FP32 gravity of the MIXED and FP32 modes flushes FP32 denormals (|x| < 1.2e-38, far below any
 # coordinate difference, mass or acceleration of the path), so rsqrtf is the bare hardware reciprocal
 # square root; FP64 arithmetic is not affected by the flag.

@@ -53,6 +53,7 @@ __global__ void k_control(const ControlParams P)
         const double err = __longlong_as_double((long long)S.err_bits);
         S.err_bits = 0ull;
         const double max_err = fabs(P.lambda * dt * err);
+        S.err_last = max_err;
         if (max_err != max_err) {
             S.status = 5;   // RED_ERR_NONFINITE
             S.halted = 1;

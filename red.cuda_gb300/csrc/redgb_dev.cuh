@@ -44,6 +44,8 @@ struct DevSys {
     int n_coll;           // collision events found for this system in the last check
     int n_ejhc;           // ejection / hit-centrum events found in the last check
     int quota;            // accepted steps still allowed (-1: unlimited)
+    int pad;
+    double err_last;      // lambda dt |error| of the last try (0 for fixed steps)
 };
 
 __host__ __device__ inline bool runnable(const DevSys& S)

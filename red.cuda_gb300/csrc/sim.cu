@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "redgb_dev.cuh"
+#include "proposer.cuh"
 #include "redgb.h"
 
 using namespace redgb;
@@ -325,6 +326,21 @@ struct red_sim {
     void pack_to_host(uint32_t s);
     std::vector<double> grid_rmax;   // largest small-body radius the collision grid was planned for
     std::vector<double> star_mass;   // the first star's effective mass the plan was made with
+    // learned step proposer (proposer.cu) and the feature log it is trained on
+    bool prop_on = false, log_on = false;
+    __nv_bfloat16* d_mlp_w = nullptr;
+    MlpNorm mlp_norm{};
+    double prop_safety = 1.0, prop_lo = 0.5, prop_hi = 2.0;
+    float* d_fpart = nullptr;
+    size_t fpart_cap = 0;
+    int* d_seg0 = nullptr;
+    int* d_nseg = nullptr;
+    float* d_feat_prev = nullptr;
+    int* d_has_prev = nullptr;
+    float* d_log = nullptr;
+    unsigned int* d_log_n = nullptr;
+    uint32_t log_cap = 0;
+    void enqueue_proposer(int& n);
 
     // plan
     std::vector<GravItem> items;
@@ -408,6 +424,8 @@ red_sim::~red_sim()
     cudaFree(d_grid); cudaFree(d_head); cudaFree(d_next); cudaFree(d_cell); cudaFree(d_fsegs);
     cudaFree(d_xfer);
     if (h_xfer) cudaFreeHost(h_xfer);
+    cudaFree(d_mlp_w); cudaFree(d_fpart); cudaFree(d_seg0); cudaFree(d_nseg); cudaFree(d_feat_prev);
+    cudaFree(d_has_prev); cudaFree(d_log); cudaFree(d_log_n);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -632,6 +650,26 @@ void red_sim::build_plan()
     upload(segs, d_segs, segs_cap);
     upload(fsegs, d_fsegs, fsegs_cap);
     upload(pairs, d_pairs, pairs_cap);
+    {
+        // each system's range of per-body segments, for the proposer's features;
+        // allocated here because the try is captured into a graph
+        std::vector<int> seg0(n_sys, 0), nseg(n_sys, 0);
+        for (size_t k = segs.size(); k-- > 0;) {
+            seg0[segs[k].sys] = (int)k;
+            nseg[segs[k].sys]++;
+        }
+        if (!d_seg0) {
+            d_seg0 = dalloc<int>(n_sys);
+            d_nseg = dalloc<int>(n_sys);
+        }
+        CK(cudaMemcpy(d_seg0, seg0.data(), n_sys * sizeof(int), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_nseg, nseg.data(), n_sys * sizeof(int), cudaMemcpyHostToDevice));
+        if (segs.size() > fpart_cap) {
+            cudaFree(d_fpart);
+            d_fpart = dalloc<float>(segs.size() * kNPart);
+            fpart_cap = segs.size();
+        }
+    }
     CK(cudaMemcpy(d_sinfo, sinfo.data(), n_sys * sizeof(SysInfo), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(d_grid, grid.data(), n_sys * sizeof(GridInfo), cudaMemcpyHostToDevice));
     table_size = table;
@@ -769,6 +807,7 @@ void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs
     launch_finish(F, (int)fsegs.size(), stream);
     mark(2);
     n++;
+    if (prop_on || log_on) enqueue_proposer(n);
     if (cfg.threshold[RED_THRESHOLD_RADII_ENHANCE_FACTOR] > 0.0) {
         CollParams Q;
         memset(&Q, 0, sizeof(Q));
@@ -777,7 +816,7 @@ void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs
         Q.mark = 1;
         launch_collision(Q, (int)pairs.size(), (int)segs.size(), use_grid, table_size, stream);
         mark(3);
-        n++;
+        n += (pairs.empty() ? 0 : 1) + (use_grid && !segs.empty() ? 2 : 0);
     }
     if (cfg.threshold[RED_THRESHOLD_EJECTION_DISTANCE] > 0.0 || cfg.threshold[RED_THRESHOLD_HIT_CENTRUM_DISTANCE] > 0.0) {
         EjhcParams E;
@@ -793,6 +832,29 @@ void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs
         n++;
     }
     launches_per_try = n;
+}
+
+// Features of the systems that accepted a try, the log record and the MLP's
+// proposal for their next step (proposer.cu).
+void red_sim::enqueue_proposer(int& n)
+{
+    FeatParams Fe;
+    memset(&Fe, 0, sizeof(Fe));
+    Fe.segs = d_segs; Fe.sinfo = d_sinfo; Fe.sys = d_sys; Fe.pos = pos_hi[0]; Fe.y_v = y_v; Fe.acc = Kv[0];
+    Fe.mass = mass; Fe.id = id; Fe.part = d_fpart;
+    launch_features(Fe, (int)segs.size(), stream);
+    ProposeParams Pp;
+    memset(&Pp, 0, sizeof(Pp));
+    Pp.n_sys = (int)n_sys; Pp.sys = d_sys; Pp.seg0 = d_seg0; Pp.nseg = d_nseg; Pp.part = d_fpart;
+    Pp.tolerance = cfg.tolerance > 0.0 ? cfg.tolerance : 1.0;
+    Pp.propose = prop_on && cfg.adaptive ? 1 : 0;
+    Pp.w = d_mlp_w; Pp.norm = mlp_norm;
+    Pp.safety = prop_safety; Pp.ratio_lo = prop_lo; Pp.ratio_hi = prop_hi; Pp.output_interval = cfg.output_interval;
+    Pp.log = log_on ? 1 : 0;
+    Pp.feat_prev = d_feat_prev; Pp.has_prev = d_has_prev; Pp.log_buf = d_log; Pp.log_n = d_log_n; Pp.log_cap = log_cap;
+    launch_propose(Pp, stream);
+    CK(cudaGetLastError());
+    n += 2;
 }
 
 void red_sim::capture()
@@ -1680,6 +1742,85 @@ int red_autotune(red_sim* sim)
     sim->build_plan();
     sim->prep_positions();
     CK(cudaStreamSynchronize(sim->stream));
+    return RED_OK;
+    GUARD_END
+}
+
+
+int red_set_step_proposer(red_sim* sim, const uint16_t* w_bf16, const red_mlp_norm_t* norm, double safety,
+                          double ratio_lo, double ratio_hi)
+{
+    if (int rc = check_sim(sim)) return rc;
+    if (!w_bf16 || !norm || !(safety > 0.0) || !(ratio_lo > 0.0) || !(ratio_hi >= ratio_lo))
+        return set_error(RED_ERR_ARG, "red_set_step_proposer: bad argument");
+    for (int c = 0; c < kFeat; c++)
+        if (!(norm->x_std[c] > 0.f)) return set_error(RED_ERR_ARG, "red_set_step_proposer: x_std must be positive");
+    if (!(norm->y_std > 0.f)) return set_error(RED_ERR_ARG, "red_set_step_proposer: y_std must be positive");
+    GUARD_BEGIN
+    CK(cudaStreamSynchronize(sim->stream));
+    if (!sim->d_mlp_w) sim->d_mlp_w = dalloc<__nv_bfloat16>(kNParam);
+    CK(cudaMemcpyAsync(sim->d_mlp_w, w_bf16, kNParam * sizeof(uint16_t), cudaMemcpyHostToDevice, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    memcpy(&sim->mlp_norm, norm, sizeof(MlpNorm));
+    sim->prop_safety = safety;
+    sim->prop_lo = ratio_lo;
+    sim->prop_hi = ratio_hi;
+    sim->prop_on = true;
+    sim->invalidate();
+    return RED_OK;
+    GUARD_END
+}
+
+int red_clear_step_proposer(red_sim* sim)
+{
+    if (int rc = check_sim(sim)) return rc;
+    GUARD_BEGIN
+    CK(cudaStreamSynchronize(sim->stream));
+    sim->prop_on = false;
+    sim->invalidate();
+    return RED_OK;
+    GUARD_END
+}
+
+int red_log_features(red_sim* sim, uint32_t capacity)
+{
+    if (int rc = check_sim(sim)) return rc;
+    GUARD_BEGIN
+    CK(cudaStreamSynchronize(sim->stream));
+    cudaFree(sim->d_log);
+    sim->d_log = nullptr;
+    sim->log_cap = 0;
+    sim->log_on = capacity > 0;
+    if (sim->log_on) {
+        sim->d_log = dalloc<float>((size_t)capacity * (kFeat + 1));
+        sim->log_cap = capacity;
+        if (!sim->d_log_n) sim->d_log_n = dalloc<unsigned int>(1);
+        if (!sim->d_feat_prev) {
+            sim->d_feat_prev = dalloc<float>((size_t)sim->n_sys * kFeat);
+            sim->d_has_prev = dalloc<int>(sim->n_sys);
+        }
+        CK(cudaMemsetAsync(sim->d_log_n, 0, sizeof(unsigned int), sim->stream));
+        CK(cudaMemsetAsync(sim->d_has_prev, 0, sim->n_sys * sizeof(int), sim->stream));
+        CK(cudaStreamSynchronize(sim->stream));
+    }
+    sim->invalidate();
+    return RED_OK;
+    GUARD_END
+}
+
+int red_get_feature_log(red_sim* sim, float* out, uint32_t cap, uint32_t* n_out, int32_t reset)
+{
+    if (int rc = check_sim(sim)) return rc;
+    if (!n_out || (cap && !out)) return set_error(RED_ERR_ARG, "red_get_feature_log: bad argument");
+    GUARD_BEGIN
+    unsigned int count = 0;
+    CK(cudaStreamSynchronize(sim->stream));
+    if (sim->d_log_n) CK(cudaMemcpy(&count, sim->d_log_n, sizeof(count), cudaMemcpyDeviceToHost));
+    const uint32_t n = std::min<uint32_t>(count, sim->log_cap);
+    *n_out = n;
+    const uint32_t k = std::min(n, cap);
+    if (k) CK(cudaMemcpy(out, sim->d_log, (size_t)k * (kFeat + 1) * sizeof(float), cudaMemcpyDeviceToHost));
+    if (reset && sim->d_log_n) CK(cudaMemset(sim->d_log_n, 0, sizeof(unsigned int)));
     return RED_OK;
     GUARD_END
 }

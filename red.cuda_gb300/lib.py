@@ -26,7 +26,9 @@ EXPORTS = ["red_create", "red_destroy", "red_step", "red_launch_tries", "red_syn
            "red_calc_dydx", "red_calc_integral", "red_calc_energy_interacting", "red_get_state",
            "red_set_state", "red_get_system_info", "red_set_dt_next", "red_rebuild_vectors",
            "red_autotune", "red_profile_try", "red_interactions_per_eval", "red_kernel_launches", "red_n_systems",
-           "red_calc_accel_noalloc", "red_last_error", "red_version"]
+           "red_calc_accel_noalloc", "red_mlp_param_count", "red_mlp_predict", "red_mlp_grad", "red_mlp_adam",
+           "red_set_step_proposer", "red_clear_step_proposer", "red_log_features", "red_get_feature_log",
+           "red_last_error", "red_version"]
 
 
 class RedError(RuntimeError):
@@ -71,6 +73,14 @@ class AccelArgs(C.Structure):
 NOALLOC_MAX_BODIES = 32768
 
 
+class MlpNorm(C.Structure):
+    """red_mlp_norm_t: normalisation of the proposer's features and target."""
+    _fields_ = [("x_mean", C.c_float * 12), ("x_std", C.c_float * 12), ("y_mean", C.c_float), ("y_std", C.c_float)]
+
+
+MLP_NFEAT = 12
+
+
 class Integral(C.Structure):
     _fields_ = [("R", C.c_double * 4), ("V", C.c_double * 4), ("C", C.c_double * 4), ("E", C.c_double)]
 
@@ -113,6 +123,14 @@ def load(path=LIB_PATH):
     L.red_n_systems.argtypes = [P]
     L.red_n_systems.restype = C.c_uint32
     L.red_calc_accel_noalloc.argtypes = [C.POINTER(AccelArgs)]
+    L.red_mlp_param_count.restype = C.c_uint32
+    L.red_mlp_predict.argtypes = [P, C.POINTER(MlpNorm), P, P, C.c_uint32, P]
+    L.red_mlp_grad.argtypes = [P, P, P, C.c_uint32, P, P, P]
+    L.red_mlp_adam.argtypes = [P, P, P, P, P, C.c_uint32, C.c_float, C.c_float, C.c_float, C.c_float, P]
+    L.red_set_step_proposer.argtypes = [P, P, C.POINTER(MlpNorm), C.c_double, C.c_double, C.c_double]
+    L.red_clear_step_proposer.argtypes = [P]
+    L.red_log_features.argtypes = [P, C.c_uint32]
+    L.red_get_feature_log.argtypes = [P, P, C.c_uint32, u32p, C.c_int32]
     L.red_last_error.restype = C.c_char_p
     L.red_version.restype = C.c_char_p
     _lib = L
@@ -131,6 +149,23 @@ def _check(rc):
 def calc_accel_noalloc(args):
     """Calls red_calc_accel_noalloc with a filled AccelArgs; raises on error."""
     _check(load().red_calc_accel_noalloc(C.byref(args)))
+
+
+def mlp_param_count():
+    return int(load().red_mlp_param_count())
+
+
+def mlp_predict(w_ptr, norm, x_ptr, out_ptr, n, stream=None):
+    """Device pointers: BF16 weights, n x 12 raw features -> n predicted log|dt|."""
+    _check(load().red_mlp_predict(w_ptr, C.byref(norm), x_ptr, out_ptr, n, stream))
+
+
+def mlp_grad(w_ptr, xn_ptr, tn_ptr, n, grad_ptr, loss_ptr, stream=None):
+    _check(load().red_mlp_grad(w_ptr, xn_ptr, tn_ptr, n, grad_ptr, loss_ptr, stream))
+
+
+def mlp_adam(master_ptr, w_ptr, m_ptr, v_ptr, grad_ptr, step, lr, beta1=0.9, beta2=0.999, eps=1e-8, stream=None):
+    _check(load().red_mlp_adam(master_ptr, w_ptr, m_ptr, v_ptr, grad_ptr, step, lr, beta1, beta2, eps, stream))
 
 
 def gas_struct(gas_record):
@@ -294,6 +329,26 @@ class Sim:
 
     def autotune(self):
         _check(load().red_autotune(self.h))
+
+    def set_step_proposer(self, w_bf16, norm, safety=1.0, ratio_lo=0.5, ratio_hi=2.0):
+        """Enables the learned proposals: w_bf16 (np.uint16, mlp_param_count()), norm (MlpNorm)."""
+        w = np.ascontiguousarray(w_bf16, np.uint16)
+        if w.size != mlp_param_count():
+            raise ValueError("expected %d BF16 parameters" % mlp_param_count())
+        _check(load().red_set_step_proposer(self.h, _p(w), C.byref(norm), safety, ratio_lo, ratio_hi))
+
+    def clear_step_proposer(self):
+        _check(load().red_clear_step_proposer(self.h))
+
+    def log_features(self, capacity):
+        _check(load().red_log_features(self.h, capacity))
+
+    def feature_log(self, cap=1 << 20, reset=False):
+        """Logged records as an (n, 13) float32 array: 12 features, log|dt| of the next accepted step."""
+        out = np.zeros((cap, MLP_NFEAT + 1), np.float32)
+        n = C.c_uint32()
+        _check(load().red_get_feature_log(self.h, _p(out), cap, C.byref(n), 1 if reset else 0))
+        return out[:min(n.value, cap)].copy()
 
     def profile_try(self, cap=64):
         """Durations (ms) and kinds of the launches of one try, run kernel by kernel."""
