@@ -9,7 +9,7 @@ A step is one try of the integrator over the disk (13 force evaluations, the
 error norm, step control, y_{n+1}, the collision check).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--config c2|c1|c3|c4|dense|cube] [--precision mixed|fp64|fp32|fp64_exact]
+                  [--config c2|c1|c3|c4|c5|dense|cube] [--precision mixed|fp64|fp32|fp64_exact]
 
 Timing: CUDA events on the integration stream around each step, L2 flushed
 (a 256 MiB write) between timed steps; value = total interactions over all
@@ -64,6 +64,13 @@ def workload(rg, name, rank=0, world=1):
         return systems, dict(integrator="rkf78", adaptive=True, tolerance=1e-10, dt=1.0 * K_GAUSS,
                              collision_factor=1.0), \
             "config4: 512 disks, N ~ U[128, 4096], 2-8 protoplanets each, RKF7(8) tol 1e-10, per-system dt"
+    if name == "c5":
+        first, count = rg.shard.ensemble_range(512, rank, world)
+        systems = ic.config4(n_systems=count, first=first)
+        return systems, dict(integrator="rkf78", adaptive=True, tolerance=1e-10, dt=1.0 * K_GAUSS,
+                             collision_factor=1.0), \
+            "config5: the config4 ensemble with learned step proposals (BF16 MLP 12-64-64-1 trained on the GPU " \
+            "on the feature log of plain runs of the same ensemble), RKF7(8) tol 1e-10"
     if name == "dense":
         s = ic.config2().relabel_all_SI()
         return [s], dict(integrator="rkf78", adaptive=True, tolerance=1e-10, dt=1.0 * K_GAUSS,
@@ -238,6 +245,48 @@ def cpu_baseline_sample(systems, kw, seconds=10.0):
             "sim_years_per_s": sim_t / K_GAUSS / YEAR / el}
 
 
+PROPOSER_WARMUP_TRIES = 400   # tries before the timed region in the learned-proposal workload
+
+
+def train_proposer(rg, systems, kw, args, local_rank, stream, log_tries=PROPOSER_WARMUP_TRIES):
+    """The proposer's training data and network: a plain run of the ensemble
+    logs (features, accepted log|dt|) records on the device; the network is
+    trained on the GPU by the library's own kernels."""
+    sim = rg.Sim(systems, precision=args.precision, device=local_rank, stream=stream.cuda_stream, **kw)
+    sim.log_features(1 << 22)
+    for _ in range(log_tries // 100):
+        sim.launch_tries(100)
+        drain_events(sim)
+    recs = sim.feature_log(cap=1 << 22)
+    sim.close()
+    t0 = time.perf_counter()
+    bits, nm, hist = rg.proposer.train(recs, epochs=30, batch=2048, lr=2e-3)
+    return {"bits": bits, "norm": nm, "records": int(len(recs)), "train_s": time.perf_counter() - t0,
+            "val_loss": hist[-1][2]}
+
+
+def plain_comparison(rg, systems, kw, args, local_rank, stream, flush):
+    """The same ensemble with the classical controller, timed the same way."""
+    import torch
+    sim = rg.Sim(systems, precision=args.precision, device=local_rank, stream=stream.cuda_stream, **kw)
+    for _ in range(max(3, args.warmup)):
+        sim.launch_tries(1)
+    drain_events(sim)
+    for _ in range(PROPOSER_WARMUP_TRIES // 100):
+        sim.launch_tries(100)
+        drain_events(sim)
+    info0 = [sim.info(k) for k in range(sim.n_systems)]
+    ms = timed_steps(torch, sim, stream, args.steps, flush)
+    drain_events(sim)
+    info1 = [sim.info(k) for k in range(sim.n_systems)]
+    sim.close()
+    tried = sum(b.n_tried - a.n_tried for a, b in zip(info0, info1))
+    failed = sum(b.n_failed - a.n_failed for a, b in zip(info0, info1))
+    sim_dt = sum(b.t - a.t for a, b in zip(info0, info1))
+    return {"rejected_fraction": failed / tried if tried else None,
+            "sim_years_per_s": sim_dt / K_GAUSS / YEAR / (ms * 1e-3), "ms_per_step": ms / args.steps}
+
+
 def run_reference(args, rg, rank, world):
     systems, kw, desc = workload(rg, args.config)
     if rank != 0:
@@ -274,13 +323,23 @@ def run_ours(args, rg, rank, world, local_rank):
     ipe = sim.interactions_per_eval
     ns = n_stage(kw)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MiB > L2
-    # warm-up (graph capture happens on the first launch)
+    proposer = None
+    if args.config == "c5":
+        proposer = train_proposer(rg, systems, kw, args, local_rank, stream)
+        sim.set_step_proposer(proposer["bits"], proposer["norm"], safety=1.0, ratio_lo=0.25, ratio_hi=4.0)
+    # warm-up (graph capture happens on the first launch); the learned-proposal
+    # workload first runs past the start-up phase its network was trained on
     for _ in range(max(3, args.warmup)):
         sim.launch_tries(1)
     drain_events(sim)
+    if proposer is not None:
+        for _ in range(PROPOSER_WARMUP_TRIES // 100):
+            sim.launch_tries(100)
+            drain_events(sim)
     E0 = sim.energy_interacting(0)
     t_before = [sim.info(k).t for k in range(sim.n_systems)]
     tried_before = sum(sim.info(k).n_tried for k in range(sim.n_systems))
+    failed_before = sum(sim.info(k).n_failed for k in range(sim.n_systems))
     launches0 = sim.kernel_launches
     clocks = ClockSampler(local_rank)
     rg.shard.barrier(local_rank)
@@ -294,6 +353,7 @@ def run_ours(args, rg, rank, world, local_rank):
     drain_events(sim)
     infos = [sim.info(k) for k in range(sim.n_systems)]
     tried = sum(i.n_tried for i in infos) - tried_before
+    failed = sum(i.n_failed for i in infos) - failed_before
     n_fail_tries = args.steps * sim.n_systems - tried  # systems that were finished / halted
     sim_dt = float(np.sum([infos[k].t - t_before[k] for k in range(sim.n_systems)]))
     E1 = sim.energy_interacting(0)
@@ -359,7 +419,8 @@ def run_ours(args, rg, rank, world, local_rank):
                            "interactions_per_eval": ipe, "evals_per_step": ns},
                 "sim_years_per_s": sim_years * world / (t_max * 1e-3),
                 "dE_over_E": dE,
-                "tries_in_timed_region": int(tried), "accept_fraction": None,
+                "tries_in_timed_region": int(tried),
+                "accept_fraction": (1.0 - failed / tried) if tried else None,
                 "e2e": {"value": e2e_value, "unit": "interactions/s", "h2d_bytes_per_step": bytes_state,
                         "d2h_bytes_per_step": bytes_state, "steps": e2e_steps,
                         "api": "red_set_state(r, v) + red_step + red_get_state(r, v)"},
@@ -369,6 +430,17 @@ def run_ours(args, rg, rank, world, local_rank):
                 "vs_plain_fp64": (value / fp64["value"]) if fp64 else None,
                 "clocks": clk,
                 "gpu_launches": int(launches)}
+        if proposer is not None:
+            plain = plain_comparison(rg, systems, kw, args, local_rank, stream, flush)
+            line["proposer"] = {
+                "records": proposer["records"], "train_s": proposer["train_s"],
+                "val_loss": proposer["val_loss"],
+                "rejected_fraction": (failed / tried) if tried else None,
+                "rejected_fraction_plain": plain["rejected_fraction"],
+                "sim_years_per_s": sim_years * world / (t_max * 1e-3),
+                "sim_years_per_s_plain": plain["sim_years_per_s"],
+                "ms_per_step_plain": plain["ms_per_step"],
+                "overhead_ms_per_try": t_max / args.steps - plain["ms_per_step"]}
         print(json.dumps(line), flush=True)
     sim.close()
 
@@ -379,7 +451,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "dense", "cube"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "dense", "cube"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp32", "fp64_exact"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")

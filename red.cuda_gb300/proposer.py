@@ -67,6 +67,9 @@ def train(records, epochs=30, batch=2048, lr=2e-3, seed=0, val_frac=0.1, device=
     import torch
     records = np.asarray(records, np.float32)
     records = records[np.isfinite(records).all(axis=1)]
+    # the device appends records in atomic order: sort them so that the split and
+    # the batches, and so the trained network, depend only on the records
+    records = records[np.lexsort(records.T[::-1])]
     if len(records) < 64:
         raise ValueError("too few records to train on: %d" % len(records))
     rng = np.random.default_rng(seed)
