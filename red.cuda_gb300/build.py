@@ -13,6 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libredgb.so")
+DRIVER = os.path.join(BUILD, "redgb_run")
 ROOT = os.path.dirname(HERE)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -40,11 +41,12 @@ def sources():
 
 def deps():
     return sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) + \
-        [os.path.join(ROOT, "include", "redgb.h"), os.path.abspath(__file__)]
+        [os.path.join(ROOT, "include", "redgb.h"), os.path.abspath(__file__),
+         os.path.join(HERE, "driver", "redgb_run.cpp")]
 
 
 def up_to_date():
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(DRIVER):
         return False
     t = os.path.getmtime(LIB)
     return all(os.path.getmtime(d) <= t for d in deps() if os.path.exists(d))
@@ -78,7 +80,21 @@ def build(force=False, verbose=False):
     cmd = [cc, "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcudart"]
     subprocess.check_call(cmd)
     os.replace(tmp, LIB)
+    build_driver(verbose)
     return LIB
+
+
+def build_driver(verbose=False):
+    """red's command-line interface over the library: _build/redgb_run."""
+    src = os.path.join(HERE, "driver", "redgb_run.cpp")
+    tmp = DRIVER + ".tmp%d" % os.getpid()
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-I" + os.path.join(ROOT, "include"), src, "-L" + BUILD, "-lredgb",
+           "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    os.replace(tmp, DRIVER)
+    return DRIVER
 
 
 if __name__ == "__main__":
