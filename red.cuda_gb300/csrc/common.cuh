@@ -4,6 +4,7 @@
 #pragma once
 #include <cfloat>
 #include <cstdio>
+#include <utility>
 
 #include "redgb_dev.cuh"
 
@@ -18,6 +19,36 @@ static __constant__ Tableau c_tb;
 // (r >= 1e-6 AU) it changes the force by < 1e-11 relative, far below FP32
 // rounding.  The FP64 paths use no softening, as red.
 constexpr float kEps2 = 1.0e-24f;
+
+// ---------------------------------------------------------------------------
+// programmatic dependent launch
+// ---------------------------------------------------------------------------
+// Every kernel of a try calls pdl_wait() in each CTA before it reads what the
+// previous kernel of the try wrote, and before it exits; then pdl_trigger().
+// So a kernel completes only after its predecessor has completed, and the
+// successor is scheduled only once every CTA of this kernel has passed its
+// wait: whatever kernels before the predecessor wrote is complete when the
+// successor starts.  Without the launch attribute both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+// Launches kernel k with the programmatic-stream-serialization attribute while
+// pdl_on() holds on this thread, as a plain launch otherwise.
+template <typename... KArgs, typename... Args>
+inline void launch_k(void (*k)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl_on() ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
 
 // ---------------------------------------------------------------------------
 // small helpers

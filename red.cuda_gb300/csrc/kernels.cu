@@ -14,6 +14,12 @@
 
 namespace redgb {
 
+namespace {
+thread_local bool t_pdl = false;
+}
+void set_pdl(bool on) { t_pdl = on; }
+bool pdl_on() { return t_pdl; }
+
 // ---------------------------------------------------------------------------
 // per-body kernels
 // ---------------------------------------------------------------------------
@@ -41,6 +47,8 @@ __global__ void __launch_bounds__(kSegment) k_prep(const Segment* segs, const Sy
 // (main.cu:471, 535-538).
 __global__ void k_control(const ControlParams P)
 {
+    pdl_wait();
+    pdl_trigger();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= P.n_sys) return;
     DevSys& S = P.sys[s];
@@ -89,6 +97,12 @@ __global__ void k_control(const ControlParams P)
 template <bool EXACT>
 __global__ void __launch_bounds__(4 * kFinishBodies) k_finish(const FinishParams P)
 {
+    pdl_wait();
+    pdl_trigger();
+    if (P.head) {   // the spatial hash of the collision check that follows starts empty
+        const long long nt = (long long)gridDim.x * blockDim.x;
+        for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < P.head_n; k += nt) P.head[k] = -1;
+    }
     const Segment sg = P.segs[blockIdx.x];
     DevSys* S = P.sys + sg.sys;
     if (S->halted) return;
@@ -177,6 +191,8 @@ __device__ __forceinline__ void collide_exact(const CollParams& P, DevSys* S, in
 __global__ void __launch_bounds__(kTile) k_collision(const CollParams P)
 {
     __shared__ float4 shi[kTile], slo[kTile];
+    pdl_wait();
+    pdl_trigger();
     const PairItem it = P.items[blockIdx.x];
     DevSys* S = P.sys + it.sys;
     if (!coll_runs(P, *S)) return;
@@ -228,6 +244,8 @@ __device__ __forceinline__ int bucket_of(int cx, int cy, int cz, int mask)
 
 __global__ void __launch_bounds__(kSegment) k_grid_insert(const CollParams P)
 {
+    pdl_wait();
+    pdl_trigger();
     const Segment sg = P.segs[blockIdx.x];
     const DevSys& S = P.sys[sg.sys];
     const GridInfo g = P.grid[sg.sys];
@@ -248,6 +266,8 @@ __global__ void __launch_bounds__(kSegment) k_grid_insert(const CollParams P)
 // dependent memory round trips as its longest list, not their sum.
 __global__ void __launch_bounds__(kSegment) k_grid_query(const CollParams P)
 {
+    pdl_wait();
+    pdl_trigger();
     const Segment sg = P.segs[blockIdx.x];
     DevSys* S = P.sys + sg.sys;
     const GridInfo g = P.grid[sg.sys];
@@ -303,6 +323,8 @@ __global__ void __launch_bounds__(kSegment) k_grid_query(const CollParams P)
 // kernel_pp_disk::check_for_ejection_hit_centrum (pp_disk.cu:283-318)
 __global__ void __launch_bounds__(kSegment) k_ejhc(const EjhcParams P)
 {
+    pdl_wait();
+    pdl_trigger();
     const Segment sg = P.segs[blockIdx.x];
     DevSys* S = P.sys + sg.sys;
     if (P.only_accepted && !S->accepted) return;
@@ -456,24 +478,25 @@ void launch_prep(const Segment* segs, int n_segs, const SysInfo* sinfo, const De
 
 void launch_control(const ControlParams& P, cudaStream_t s)
 {
-    k_control<<<(P.n_sys + 127) / 128, 128, 0, s>>>(P);
+    launch_k(k_control, (unsigned)((P.n_sys + 127) / 128), 128u, s, P);
 }
 
 void launch_finish(const FinishParams& P, int n_segs, cudaStream_t s)
 {
     if (n_segs <= 0) return;
-    if (P.stage_exact) k_finish<true><<<n_segs, 4 * kFinishBodies, 0, s>>>(P);
-    else k_finish<false><<<n_segs, 4 * kFinishBodies, 0, s>>>(P);
+    if (P.stage_exact) launch_k(k_finish<true>, (unsigned)n_segs, 4u * kFinishBodies, s, P);
+    else launch_k(k_finish<false>, (unsigned)n_segs, 4u * kFinishBodies, s, P);
 }
 
+// head_cleared: the bucket heads were set to -1 by the preceding k_finish.
 void launch_collision(const CollParams& P, int n_items, int n_segs, bool use_grid, size_t table_size,
-                      cudaStream_t s)
+                      bool head_cleared, cudaStream_t s)
 {
-    if (n_items > 0) k_collision<<<n_items, kTile, 0, s>>>(P);
+    if (n_items > 0) launch_k(k_collision, (unsigned)n_items, (unsigned)kTile, s, P);
     if (use_grid && n_segs > 0) {
-        cudaMemsetAsync(P.head, 0xff, table_size * sizeof(int), s);
-        k_grid_insert<<<n_segs, kSegment, 0, s>>>(P);
-        k_grid_query<<<n_segs, kSegment, 0, s>>>(P);
+        if (!head_cleared) cudaMemsetAsync(P.head, 0xff, table_size * sizeof(int), s);
+        launch_k(k_grid_insert, (unsigned)n_segs, (unsigned)kSegment, s, P);
+        launch_k(k_grid_query, (unsigned)n_segs, (unsigned)kSegment, s, P);
     }
 }
 
@@ -498,7 +521,7 @@ void launch_unpack_state(int o, int n, int what, const double* rvp, const int* i
 
 void launch_ejhc(const EjhcParams& P, int n_segs, cudaStream_t s)
 {
-    if (n_segs > 0) k_ejhc<<<n_segs, kSegment, 0, s>>>(P);
+    if (n_segs > 0) launch_k(k_ejhc, (unsigned)n_segs, (unsigned)kSegment, s, P);
 }
 
 void launch_potential(const Segment* segs, int n_segs, const SysInfo* sinfo, const double* y_r,

@@ -69,6 +69,8 @@ __global__ void __launch_bounds__(kSegment) k_feat_seg(const FeatParams P)
 {
     __shared__ float hx[kMaxHill], hy[kMaxHill], hz[kMaxHill], hr[kMaxHill];
     __shared__ float red[kNPart][kSegment / 32];
+    pdl_wait();
+    pdl_trigger();
     const Segment sg = P.segs[blockIdx.x];
     const DevSys& S = P.sys[sg.sys];
     if (!S.accepted) return;   // uniform
@@ -180,6 +182,8 @@ __device__ __forceinline__ void normalise(const MlpNorm& nm, const float (&f)[kF
 // partials (fixed order), the log record, the proposal.
 __global__ void k_propose(const ProposeParams P)
 {
+    pdl_wait();
+    pdl_trigger();
     const int lane = threadIdx.x & 31;
     const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (s >= P.n_sys) return;
@@ -386,12 +390,12 @@ __global__ void k_adam(float* master, __nv_bfloat16* w, float* m, float* v, cons
 
 void launch_features(const FeatParams& F, int n_segs, cudaStream_t s)
 {
-    if (n_segs > 0) k_feat_seg<<<n_segs, kSegment, 0, s>>>(F);
+    if (n_segs > 0) launch_k(k_feat_seg, (unsigned)n_segs, (unsigned)kSegment, s, F);
 }
 
 void launch_propose(const ProposeParams& P, cudaStream_t s)
 {
-    if (P.n_sys > 0) k_propose<<<(P.n_sys + 3) / 4, 128, 0, s>>>(P);
+    if (P.n_sys > 0) launch_k(k_propose, (unsigned)((P.n_sys + 3) / 4), 128u, s, P);
 }
 
 }  // namespace redgb

@@ -177,6 +177,8 @@ struct FinishParams {
     const int* id;
     float4* pos_hi0;
     float4* pos_lo0;
+    int* head;                // spatial-hash bucket heads, set to -1 here when not null
+    long long head_n;
 };
 
 struct ControlParams {
@@ -241,6 +243,12 @@ void plan_gravity_items(const SysInfo& si, int sys, int mode, int chunk_override
 // fixes the arithmetic of the stage combinations: FP64_EXACT combines in red's
 // operation order without FMA, the other modes with FMA.
 void set_tableau(const Tableau& tb, cudaStream_t s);
+// Programmatic dependent launch of the kernels of a try (kernels.cu): while set
+// on the calling thread, the launchers give each kernel the
+// programmatic-stream-serialization attribute, so that it is scheduled while
+// its predecessor runs and waits for it with griddepcontrol.wait.
+void set_pdl(bool on);
+bool pdl_on();
 void launch_stage(const StageParams& P, int n_items, int mode, cudaStream_t s);
 int stage_variant(const StageParams& P);
 void set_tableau_mixed(const Tableau& tb, cudaStream_t s);
@@ -257,7 +265,7 @@ void launch_prep(const Segment* segs, int n_segs, const SysInfo* sinfo, const De
 void launch_control(const ControlParams& P, cudaStream_t s);
 void launch_finish(const FinishParams& P, int n_segs, cudaStream_t s);
 void launch_collision(const CollParams& P, int n_items, int n_segs, bool use_grid, size_t table_size,
-                      cudaStream_t s);
+                      bool head_cleared, cudaStream_t s);
 void launch_ejhc(const EjhcParams& P, int n_segs, cudaStream_t s);
 void launch_pack_state(int o, int n, const double* y_r, const double* y_v, const double* mass, const double* radius,
                        const double* density, const double* cd, const int* id, const int* btype, double* rvp,

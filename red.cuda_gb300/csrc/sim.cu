@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -804,17 +805,22 @@ void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs
     F.id = id;
     F.pos_hi0 = pos_hi[0];
     F.pos_lo0 = pos_lo[0];
+    const bool coll = cfg.threshold[RED_THRESHOLD_RADII_ENHANCE_FACTOR] > 0.0;
+    if (coll && use_grid && !segs.empty()) {
+        F.head = d_head;
+        F.head_n = (long long)table_size;
+    }
     launch_finish(F, (int)fsegs.size(), stream);
     mark(2);
     n++;
     if (prop_on || log_on) enqueue_proposer(n);
-    if (cfg.threshold[RED_THRESHOLD_RADII_ENHANCE_FACTOR] > 0.0) {
+    if (coll) {
         CollParams Q;
         memset(&Q, 0, sizeof(Q));
         fill_coll(Q);
         Q.only_accepted = 1;
         Q.mark = 1;
-        launch_collision(Q, (int)pairs.size(), (int)segs.size(), use_grid, table_size, stream);
+        launch_collision(Q, (int)pairs.size(), (int)segs.size(), use_grid, table_size, F.head != nullptr, stream);
         mark(3);
         n += (pairs.empty() ? 0 : 1) + (use_grid && !segs.empty() ? 2 : 0);
     }
@@ -862,7 +868,19 @@ void red_sim::capture()
     if (graph) return;
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_try();
+    // the kernels of the try are chained by programmatic dependent launch
+    // (REDGB_PDL=0 captures plain launches)
+    const char* pe = getenv("REDGB_PDL");
+    set_pdl(!(pe && pe[0] == '0'));
+    try {
+        enqueue_try();
+    } catch (...) {
+        set_pdl(false);
+        cudaStreamEndCapture(stream, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    set_pdl(false);
     cudaError_t e = cudaStreamEndCapture(stream, &g);
     if (e != cudaSuccess) throw CudaError{e, "cudaStreamEndCapture", __LINE__};
     e = cudaGraphInstantiate(&graph, g, 0);
@@ -1323,7 +1341,7 @@ static int check_generic(red_sim* sim, int collision, red_event_t* out, uint32_t
         Q.only_accepted = 0;
         Q.mark = 0;
         sim->prep_positions();
-        launch_collision(Q, (int)sim->pairs.size(), (int)sim->segs.size(), sim->use_grid, sim->table_size,
+        launch_collision(Q, (int)sim->pairs.size(), (int)sim->segs.size(), sim->use_grid, sim->table_size, false,
                          sim->stream);
     } else {
         EjhcParams E;

@@ -352,15 +352,64 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
     __shared__ double ops[O::N][kMaxElem];
     const GravItem it = P.items[blockIdx.x];
     const int s = P.stage;
+    // Stage 0 follows the kernels that update the system records, y and the
+    // stage-0 positions, and waits first.  A later stage reads before its wait
+    // only what the previous stage does not write: the system record (written
+    // after the last stage), y, ids, masses, K_q of stages <= s - 2 (the stage
+    // velocity Kr[q] is written by stage q - 1, the acceleration Kv[q] by q).
+    if (s == 0) pdl_wait();
     DevSys* S = P.sys + it.sys;
     double tsys = 0.0, dt = 0.0;
     if (!P.standalone) {
         const int act = S->active, hal = S->halted, quo = S->quota;
         tsys = S->t;
         dt = S->dt_try;
-        if (!(act && !hal && quo != 0)) return;   // uniform over the CTA
+        if (!(act && !hal && quo != 0)) {   // uniform over the CTA
+            pdl_wait();
+            return;
+        }
     }
     const int t = threadIdx.x;
+
+    // ---- the element of the epilogue; its operands go to shared memory ----
+    const int nel = 3 * it.nsink;
+    const bool elem = t < nel;
+    const int ke = elem ? t / 3 : 0;
+    const int ce = elem ? t % 3 : 0;
+    const int ie = it.sink0 + ke;
+    const int x = 3 * ie + ce;
+    const int idi = P.id[ie];
+    const bool drag_on = P.gas.enabled && it.cls == CLS_NSI;
+    const bool need_vs = drag_on || V != 0;
+    if (elem) {   // copy group 0: the operands older than the previous stage
+        if constexpr (V >= 1 && V <= 14) {
+            cp_async8(&ops[O::YR][t], P.y_r + x);
+            cp_async8(&ops[O::YV][t], P.y_v + x);
+        }
+#pragma unroll
+        for (int q = 0; q < O::nk; q++) {
+            const int src = op_src<V>(q);
+            if (src != s) cp_async8(&ops[O::KR + q][t], P.Kr[src] + x);
+            if (!(kRkf && src == V - 1) && src != s - 1) cp_async8(&ops[O::KV + q][t], P.Kv[src] + x);
+        }
+    }
+    cp_async_commit();
+    // ---- the stars' masses for the central-star term (FP32 modes), double-single ----
+    const bool star_term = kF32 && it.nstar > 0;
+    const int nst0 = star_term ? min(kStarBatch, it.nstar) : 0;
+    if (t < nst0) {
+        if (t == 0 && it.mstar_set) {
+            sm.star_m[0] = make_float2(it.mstar_hi, it.mstar_lo);
+        } else {
+            const int j = it.soff + t;
+            const double m = P.id[j] < 0 ? 0.0 : P.mass[j];
+            const float mh = __double2float_rn(m);
+            sm.star_m[t] = make_float2(mh, __double2float_rn(m - (double)mh));
+        }
+    }
+
+    pdl_wait();
+    pdl_trigger();
 
     // ---- first source tile, into registers ----
     float4 th = make_float4(0.f, 0.f, 0.f, 0.f), tl = th;
@@ -381,17 +430,7 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
             td = D4{P.r_in[3 * j], P.r_in[3 * j + 1], P.r_in[3 * j + 2], (MODE == MODE_FP64 && tid < 0) ? 0.0 : m};
         }
     }
-
-    // ---- the element of the epilogue; its operands go to shared memory ----
-    const int nel = 3 * it.nsink;
-    const bool elem = t < nel;
-    const int ke = elem ? t / 3 : 0;
-    const int ce = elem ? t % 3 : 0;
-    const int ie = it.sink0 + ke;
-    const int x = 3 * ie + ce;
-    const int idi = P.id[ie];
-    const bool drag_on = P.gas.enabled && it.cls == CLS_NSI;
-    const bool need_vs = drag_on || V != 0;
+    // copy group A: the positions of this stage
     if (kF32) {
         if (t < it.nsink) {
             cp_async16(&sm.snk.f.hi[t], P.pos_hi_in + it.sink0 + t);
@@ -411,17 +450,13 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
         cp_async8(&sm.snk.d[t], P.r_in + 3 * it.sink0 + t);
     }
     cp_async_commit();
-    if (elem) {
+    if (elem) {   // copy group B: the operands the previous stage wrote
         if (need_vs) cp_async8(&ops[O::VS][t], P.Kr[s] + x);
-        if constexpr (V >= 1 && V <= 14) {
-            cp_async8(&ops[O::YR][t], P.y_r + x);
-            cp_async8(&ops[O::YV][t], P.y_v + x);
-        }
 #pragma unroll
         for (int q = 0; q < O::nk; q++) {
             const int src = op_src<V>(q);
-            cp_async8(&ops[O::KR + q][t], P.Kr[src] + x);
-            if (!(kRkf && src == V - 1)) cp_async8(&ops[O::KV + q][t], P.Kv[src] + x);
+            if (src == s) cp_async8(&ops[O::KR + q][t], P.Kr[src] + x);
+            if (!(kRkf && src == V - 1) && src == s - 1) cp_async8(&ops[O::KV + q][t], P.Kv[src] + x);
         }
     }
     cp_async_commit();
@@ -443,19 +478,6 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
         sm.sc[t][0] = f;
         sm.sc[t][1] = gx;
         sm.sc[t][2] = gy;
-    }
-    // ---- the stars' masses for the central-star term (FP32 modes), double-single ----
-    const bool star_term = kF32 && it.nstar > 0;
-    const int nst0 = star_term ? min(kStarBatch, it.nstar) : 0;
-    if (t < nst0) {
-        if (t == 0 && it.mstar_set) {
-            sm.star_m[0] = make_float2(it.mstar_hi, it.mstar_lo);
-        } else {
-            const int j = it.soff + t;
-            const double m = P.id[j] < 0 ? 0.0 : P.mass[j];
-            const float mh = __double2float_rn(m);
-            sm.star_m[t] = make_float2(mh, __double2float_rn(m - (double)mh));
-        }
     }
     if (kF32) {
         if (!staged) {
@@ -642,23 +664,23 @@ template <int MODE, bool EXACT>
 void launch_stage_variant(const StageParams& P, int n, int v, cudaStream_t s)
 {
     switch (v) {
-    case 1: k_stage<MODE, EXACT, 1><<<n, kTile, 0, s>>>(P); break;
-    case 2: k_stage<MODE, EXACT, 2><<<n, kTile, 0, s>>>(P); break;
-    case 3: k_stage<MODE, EXACT, 3><<<n, kTile, 0, s>>>(P); break;
-    case 4: k_stage<MODE, EXACT, 4><<<n, kTile, 0, s>>>(P); break;
-    case 5: k_stage<MODE, EXACT, 5><<<n, kTile, 0, s>>>(P); break;
-    case 6: k_stage<MODE, EXACT, 6><<<n, kTile, 0, s>>>(P); break;
-    case 7: k_stage<MODE, EXACT, 7><<<n, kTile, 0, s>>>(P); break;
-    case 8: k_stage<MODE, EXACT, 8><<<n, kTile, 0, s>>>(P); break;
-    case 9: k_stage<MODE, EXACT, 9><<<n, kTile, 0, s>>>(P); break;
-    case 10: k_stage<MODE, EXACT, 10><<<n, kTile, 0, s>>>(P); break;
-    case 11: k_stage<MODE, EXACT, 11><<<n, kTile, 0, s>>>(P); break;
-    case 12: k_stage<MODE, EXACT, 12><<<n, kTile, 0, s>>>(P); break;
-    case 13: k_stage<MODE, EXACT, 13><<<n, kTile, 0, s>>>(P); break;
-    case 14: k_stage<MODE, EXACT, 14><<<n, kTile, 0, s>>>(P); break;
-    case 15: k_stage<MODE, EXACT, 15><<<n, kTile, 0, s>>>(P); break;
-    case 16: k_stage<MODE, EXACT, 16><<<n, kTile, 0, s>>>(P); break;
-    default: k_stage<MODE, EXACT, 0><<<n, kTile, 0, s>>>(P); break;
+    case 1: launch_k(k_stage<MODE, EXACT, 1>, n, kTile, s, P); break;
+    case 2: launch_k(k_stage<MODE, EXACT, 2>, n, kTile, s, P); break;
+    case 3: launch_k(k_stage<MODE, EXACT, 3>, n, kTile, s, P); break;
+    case 4: launch_k(k_stage<MODE, EXACT, 4>, n, kTile, s, P); break;
+    case 5: launch_k(k_stage<MODE, EXACT, 5>, n, kTile, s, P); break;
+    case 6: launch_k(k_stage<MODE, EXACT, 6>, n, kTile, s, P); break;
+    case 7: launch_k(k_stage<MODE, EXACT, 7>, n, kTile, s, P); break;
+    case 8: launch_k(k_stage<MODE, EXACT, 8>, n, kTile, s, P); break;
+    case 9: launch_k(k_stage<MODE, EXACT, 9>, n, kTile, s, P); break;
+    case 10: launch_k(k_stage<MODE, EXACT, 10>, n, kTile, s, P); break;
+    case 11: launch_k(k_stage<MODE, EXACT, 11>, n, kTile, s, P); break;
+    case 12: launch_k(k_stage<MODE, EXACT, 12>, n, kTile, s, P); break;
+    case 13: launch_k(k_stage<MODE, EXACT, 13>, n, kTile, s, P); break;
+    case 14: launch_k(k_stage<MODE, EXACT, 14>, n, kTile, s, P); break;
+    case 15: launch_k(k_stage<MODE, EXACT, 15>, n, kTile, s, P); break;
+    case 16: launch_k(k_stage<MODE, EXACT, 16>, n, kTile, s, P); break;
+    default: launch_k(k_stage<MODE, EXACT, 0>, n, kTile, s, P); break;
     }
 }
 
