@@ -199,6 +199,9 @@ uint64_t red_interactions_per_eval(red_sim* sim);
 /* Kernel launches made by the library since creation (for launch accounting). */
 uint64_t red_kernel_launches(red_sim* sim);
 uint32_t red_n_systems(red_sim* sim);
+/* Records in system sys's arrays (n_total of red_get_system_info), from host
+   bookkeeping: no device synchronisation.  0 for a bad handle or index. */
+uint32_t red_n_bodies(red_sim* sim, uint32_t sys);
 
 /* ---- allocation-free gravity ---------------------------------------------
  * No counterpart in red.  For callers that cannot call cudaMalloc (device

@@ -416,8 +416,11 @@ __global__ void k_pack_state(int o, int n, const double* y_r, const double* y_v,
 }
 
 // Inverse of k_pack_state for the parts named in `what` (1 r, 2 v, 4 p, 8 id).
+// New positions also go to the FP32 copies of stage 0 (x, y, z; the .w words
+// follow mass and radius and are set by k_prep).
 __global__ void k_unpack_state(int o, int n, int what, const double* rvp, const int* ib, double* y_r, double* y_v,
-                               double* mass, double* radius, double* density, double* cd, int* id)
+                               double* mass, double* radius, double* density, double* cd, int* id, float4* hi0,
+                               float4* lo0)
 {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n && (what & 8)) id[o + k] = ib[2 * k];
@@ -427,7 +430,10 @@ __global__ void k_unpack_state(int o, int n, int what, const double* rvp, const 
     const int w = (int)(k - seg * 4LL * n);
     const int i = o + w / 4, c = w % 4;
     const double v = rvp[k];
-    if (seg == 0) { if (c < 3) y_r[3 * i + c] = v; }
+    if (seg == 0) {
+        if (c < 3) y_r[3 * i + c] = v;
+        write_pos_c(hi0, lo0, i, c, v);
+    }
     else if (seg == 1) { if (c < 3) y_v[3 * i + c] = v; }
     else if (c == 0) mass[i] = v;
     else if (c == 1) radius[i] = v;
@@ -435,9 +441,21 @@ __global__ void k_unpack_state(int o, int n, int what, const double* rvp, const 
     else cd[i] = v;
 }
 
+// Sets the try quota of every system (red_step: 1 accepted step, then -1 = none).
+__global__ void k_set_quota(DevSys* sys, int n_sys, int q)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n_sys) sys[s].quota = q;
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+void launch_set_quota(DevSys* sys, int n_sys, int q, cudaStream_t s)
+{
+    if (n_sys > 0) k_set_quota<<<(unsigned)((n_sys + 127) / 128), 128, 0, s>>>(sys, n_sys, q);
+}
+
 void set_tableau(const Tableau& tb, cudaStream_t s)
 {
     cudaMemcpyToSymbolAsync(c_tb, &tb, sizeof(Tableau), 0, cudaMemcpyHostToDevice, s);
@@ -511,12 +529,13 @@ void launch_pack_state(int o, int n, const double* y_r, const double* y_v, const
 }
 
 void launch_unpack_state(int o, int n, int what, const double* rvp, const int* ib, double* y_r, double* y_v,
-                         double* mass, double* radius, double* density, double* cd, int* id, cudaStream_t s)
+                         double* mass, double* radius, double* density, double* cd, int* id, float4* hi0,
+                         float4* lo0, cudaStream_t s)
 {
     if (n <= 0) return;
     const long long tot = 12LL * n;
     k_unpack_state<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(o, n, what, rvp, ib, y_r, y_v, mass, radius,
-                                                                 density, cd, id);
+                                                                 density, cd, id, hi0, lo0);
 }
 
 void launch_ejhc(const EjhcParams& P, int n_segs, cudaStream_t s)

@@ -267,11 +267,13 @@ void launch_finish(const FinishParams& P, int n_segs, cudaStream_t s);
 void launch_collision(const CollParams& P, int n_items, int n_segs, bool use_grid, size_t table_size,
                       bool head_cleared, cudaStream_t s);
 void launch_ejhc(const EjhcParams& P, int n_segs, cudaStream_t s);
+void launch_set_quota(DevSys* sys, int n_sys, int q, cudaStream_t s);
 void launch_pack_state(int o, int n, const double* y_r, const double* y_v, const double* mass, const double* radius,
                        const double* density, const double* cd, const int* id, const int* btype, double* rvp,
                        int* ib, cudaStream_t s);
 void launch_unpack_state(int o, int n, int what, const double* rvp, const int* ib, double* y_r, double* y_v,
-                         double* mass, double* radius, double* density, double* cd, int* id, cudaStream_t s);
+                         double* mass, double* radius, double* density, double* cd, int* id, float4* hi0,
+                         float4* lo0, cudaStream_t s);
 void launch_potential(const Segment* segs, int n_segs, const SysInfo* sinfo, const double* y_r,
                       const double* mass, const int* id, int sys_filter, int interacting, double* u,
                       cudaStream_t s);

@@ -1296,27 +1296,36 @@ int red_step(red_sim* sim, double* dt_did)
     if (int rc = check_sim(sim)) return rc;
     GUARD_BEGIN
     std::vector<DevSys> ds;
-    sim->read_sys(ds);
-    for (DevSys& d : ds) d.quota = 1;
-    sim->write_sys(ds);
-    // each try is one graph launch; systems stop after one accepted step
+    // Each try is one graph launch, followed by one read of the system records
+    // (the only host synchronisation).  Several systems get a quota of one
+    // accepted step, so that those done wait for the others; a single system
+    // just stops being launched once its try is accepted.
+    const bool quota = sim->n_sys > 1;
+    if (quota) {
+        launch_set_quota(sim->d_sys, (int)sim->n_sys, 1, sim->stream);
+        CK(cudaGetLastError());
+        sim->launches++;
+    }
     for (int guard = 0; guard < 100000; guard++) {
         sim->launch_tries(1);
         sim->read_sys(ds);
         bool pending = false;
         for (const DevSys& d : ds) {
             if (d.status) {
-                for (DevSys& q : ds) q.quota = -1;
-                sim->write_sys(ds);
+                if (quota) launch_set_quota(sim->d_sys, (int)sim->n_sys, -1, sim->stream);
+                CK(cudaStreamSynchronize(sim->stream));
                 return set_error(d.status, "integration stopped: status %d", d.status);
             }
-            if (d.active && !d.halted && d.quota != 0) pending = true;
+            if (d.active && !d.halted && (quota ? d.quota != 0 : !d.accepted)) pending = true;
         }
         if (!pending) break;
     }
     if (dt_did) *dt_did = ds[0].dt_did;
-    for (DevSys& d : ds) d.quota = -1;
-    sim->write_sys(ds);
+    if (quota) {
+        launch_set_quota(sim->d_sys, (int)sim->n_sys, -1, sim->stream);
+        CK(cudaGetLastError());
+        sim->launches++;
+    }
     return RED_OK;
     GUARD_END
 }
@@ -1555,14 +1564,24 @@ int red_get_state(red_sim* sim, uint32_t sys, red_var4_t* r, red_var4_t* v, red_
     if (int rc = check_sim(sim)) return rc;
     if (sys >= sim->n_sys) return set_error(RED_ERR_ARG, "bad system index");
     GUARD_BEGIN
-    sim->pack_to_host(sys);
+    // packed on the device, then copied straight into the caller's arrays (no
+    // staging copy on the host; pinned caller memory gets a direct DMA)
     const SysHost& h = sim->sh[sys];
     const size_t n = h.n;
-    const double* rvp = (const double*)sim->h_xfer;
-    const int* ib = (const int*)(sim->h_xfer + 12 * n * sizeof(double));
-    if (r) memcpy(r, rvp, n * sizeof(red_var4_t));
-    if (v) memcpy(v, rvp + 4 * n, n * sizeof(red_var4_t));
-    if (p) memcpy(p, rvp + 8 * n, n * sizeof(red_param_t));
+    sim->ensure_xfer(xfer_bytes(n));
+    const double* d_rvp = (const double*)sim->d_xfer;
+    const size_t ib_off = 12 * n * sizeof(double);
+    launch_pack_state((int)h.off, (int)n, sim->y_r, sim->y_v, sim->mass, sim->radius, sim->density, sim->cd,
+                      sim->id, sim->btype, (double*)sim->d_xfer, (int*)(sim->d_xfer + ib_off), sim->stream);
+    CK(cudaGetLastError());
+    sim->launches++;
+    const cudaMemcpyKind d2h = cudaMemcpyDeviceToHost;
+    if (r) CK(cudaMemcpyAsync(r, d_rvp, n * sizeof(red_var4_t), d2h, sim->stream));
+    if (v) CK(cudaMemcpyAsync(v, d_rvp + 4 * n, n * sizeof(red_var4_t), d2h, sim->stream));
+    if (p) CK(cudaMemcpyAsync(p, d_rvp + 8 * n, n * sizeof(red_param_t), d2h, sim->stream));
+    if (md) CK(cudaMemcpyAsync(sim->h_xfer + ib_off, sim->d_xfer + ib_off, 2 * n * sizeof(int), d2h, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    const int* ib = (const int*)(sim->h_xfer + ib_off);
     if (md) {
         for (size_t i = 0; i < n; i++) {
             md[i].id = ib[2 * i];
@@ -1584,33 +1603,36 @@ int red_set_state(red_sim* sim, uint32_t sys, const red_var4_t* r, const red_var
     const SysHost& h = sim->sh[sys];
     const size_t n = h.n;
     sim->ensure_xfer(xfer_bytes(n));
-    double* rvp = (double*)sim->h_xfer;
-    int* ib = (int*)(sim->h_xfer + 12 * n * sizeof(double));
+    const size_t ib_off = 12 * n * sizeof(double);
+    int* ib = (int*)(sim->h_xfer + ib_off);
     if (md) {
         // body types are fixed by the class ranges: read the current ones first
         sim->pack_to_host(sys);
         for (size_t i = 0; i < n; i++)
             if (md[i].body_type != ib[2 * i + 1])
                 return set_error(RED_ERR_ARG, "body types cannot change through red_set_state");
-    } else {
-        CK(cudaStreamSynchronize(sim->stream));   // h_xfer may still feed a transfer
     }
+    // the caller's arrays go straight to the device (no staging copy on the
+    // host; pinned caller memory gets a direct DMA); only the ids pass through
+    // the pinned staging buffer
+    double* d_rvp = (double*)sim->d_xfer;
+    const cudaMemcpyKind h2d = cudaMemcpyHostToDevice;
     int what = 0;
-    if (r) { memcpy(rvp, r, n * sizeof(red_var4_t)); what |= 1; }
-    if (v) { memcpy(rvp + 4 * n, v, n * sizeof(red_var4_t)); what |= 2; }
-    if (p) { memcpy(rvp + 8 * n, p, n * sizeof(red_param_t)); what |= 4; }
+    if (r) { CK(cudaMemcpyAsync(d_rvp, r, n * sizeof(red_var4_t), h2d, sim->stream)); what |= 1; }
+    if (v) { CK(cudaMemcpyAsync(d_rvp + 4 * n, v, n * sizeof(red_var4_t), h2d, sim->stream)); what |= 2; }
+    if (p) { CK(cudaMemcpyAsync(d_rvp + 8 * n, p, n * sizeof(red_param_t), h2d, sim->stream)); what |= 4; }
     if (md) {
         for (size_t i = 0; i < n; i++) {
             ib[2 * i] = md[i].id;
             sim->mig_type[h.off + i] = md[i].mig_type;
             sim->mig_stop_at[h.off + i] = md[i].mig_stop_at;
         }
+        CK(cudaMemcpyAsync(sim->d_xfer + ib_off, ib, 2 * n * sizeof(int), h2d, sim->stream));
         what |= 8;
     }
-    CK(cudaMemcpyAsync(sim->d_xfer, sim->h_xfer, xfer_bytes(n), cudaMemcpyHostToDevice, sim->stream));
     launch_unpack_state((int)h.off, (int)n, what, (const double*)sim->d_xfer,
                         (const int*)(sim->d_xfer + 12 * n * sizeof(double)), sim->y_r, sim->y_v, sim->mass,
-                        sim->radius, sim->density, sim->cd, sim->id, sim->stream);
+                        sim->radius, sim->density, sim->cd, sim->id, sim->pos_hi[0], sim->pos_lo[0], sim->stream);
     CK(cudaGetLastError());
     sim->launches++;
     bool replan = false;
@@ -1627,7 +1649,9 @@ int red_set_state(red_sim* sim, uint32_t sys, const red_var4_t* r, const red_var
         CK(cudaStreamSynchronize(sim->stream));
         sim->build_plan();
     }
-    sim->prep_positions();
+    // new positions alone are already in the FP32 copies (k_unpack_state);
+    // masses, radii and ids change their .w words
+    if (p || md || replan) sim->prep_positions();
     CK(cudaStreamSynchronize(sim->stream));
     return RED_OK;
     GUARD_END
@@ -1720,6 +1744,7 @@ int red_profile_try(red_sim* sim, float* ms, int32_t* kind, uint32_t cap, uint32
 uint64_t red_interactions_per_eval(red_sim* sim) { return sim ? sim->interactions_per_eval() : 0; }
 uint64_t red_kernel_launches(red_sim* sim) { return sim ? sim->launches : 0; }
 uint32_t red_n_systems(red_sim* sim) { return sim ? sim->n_sys : 0; }
+uint32_t red_n_bodies(red_sim* sim, uint32_t sys) { return sim && sys < sim->n_sys ? sim->sh[sys].n : 0; }
 
 int red_autotune(red_sim* sim)
 {

@@ -26,6 +26,7 @@ EXPORTS = ["red_create", "red_destroy", "red_step", "red_launch_tries", "red_syn
            "red_calc_dydx", "red_calc_integral", "red_calc_energy_interacting", "red_get_state",
            "red_set_state", "red_get_system_info", "red_set_dt_next", "red_rebuild_vectors",
            "red_autotune", "red_profile_try", "red_interactions_per_eval", "red_kernel_launches", "red_n_systems",
+           "red_n_bodies",
            "red_calc_accel_noalloc", "red_mlp_param_count", "red_mlp_predict", "red_mlp_grad", "red_mlp_adam",
            "red_set_step_proposer", "red_clear_step_proposer", "red_log_features", "red_get_feature_log",
            "red_last_error", "red_version"]
@@ -122,6 +123,8 @@ def load(path=LIB_PATH):
     L.red_kernel_launches.restype = C.c_uint64
     L.red_n_systems.argtypes = [P]
     L.red_n_systems.restype = C.c_uint32
+    L.red_n_bodies.argtypes = [P, C.c_uint32]
+    L.red_n_bodies.restype = C.c_uint32
     L.red_calc_accel_noalloc.argtypes = [C.POINTER(AccelArgs)]
     L.red_mlp_param_count.restype = C.c_uint32
     L.red_mlp_predict.argtypes = [P, C.POINTER(MlpNorm), P, P, C.c_uint32, P]
@@ -297,11 +300,12 @@ class Sim:
         """System `sys` as a System; with `out`, the arrays named in `parts`
         (r, v, p, m = metadata) are written into out's arrays in place (which
         must be contiguous and hold n_total records) and out is returned."""
-        info = self.info(sys)
-        n = info.n_total
         if out is None:
+            info = self.info(sys)
+            n = info.n_total
             r, v, p, md = np.zeros(n, VAR4), np.zeros(n, VAR4), np.zeros(n, PARAM), np.zeros(n, BMD)
         else:
+            n = load().red_n_bodies(self.h, sys)
             r, v, p, md = out.r, out.v, out.p, out.md
             for a in (r, v, p, md):
                 if not a.flags["C_CONTIGUOUS"] or len(a) != n:
