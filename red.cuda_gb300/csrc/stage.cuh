@@ -7,17 +7,18 @@
 // combination that gives the positions of the next stage (or the error norm
 // after the last stage).
 //
-// The kernel is instantiated per arithmetic mode and per "variant" V, the
-// shape of the next-stage combination:
+// The kernel is instantiated per arithmetic mode; the "variant" V, the shape
+// of the next-stage combination, is a launch argument:
 //   V = 0        no combination (standalone evaluation, last stage of a try)
 //   V = 1 .. 12  RKF7(8) stage V: y + dt * sum_q a_{V,q} K_q
 //   V = 13       RK4 stage s + 1: y + (a_{s+1} dt) K_s
 //   V = 14       RK4 y_{n+1} as the input of the adaptive stage 4
 //   V = 15       RKF7(8) error norm after stage 12
 //   V = 16       RK4 error norm after stage 4
-// With V known at compile time the operands of the combination are loaded
-// into registers at the start of the kernel, overlapping the gravity loop.
-// Each mode lives in its own translation unit (stage_*.cu).
+// The operands of the combination are copied into shared memory at the start
+// of the kernel, overlapping the gravity loop.  One kernel body serves all
+// stages, so after the first stage of a try its code is cached.  Each mode
+// lives in its own translation unit (stage_*.cu).
 #pragma once
 #include "common.cuh"
 
@@ -129,17 +130,26 @@ __host__ __device__ constexpr int var_nk(int v)
     return v == 1 ? 1 : v == 2 ? 2 : v == 3 ? 2 : v == 4 ? 3 : v == 5 ? 3 : v == 6 ? 4 : v == 7 ? 4 : v == 8 ? 6
          : v == 9 ? 7 : v == 10 ? 8 : v == 11 ? 6 : v == 12 ? 9 : (v == 14 || v == 15) ? 3 : v == 16 ? 1 : 0;
 }
-template <int V> struct Ops {
-    static constexpr int nk = var_nk(V);
-    static constexpr int VS = 0, YR = 1, YV = 2, KR = 3, KV = 3 + nk, N = 3 + 2 * nk;
+constexpr int kNkMax = 9;                  // the most K operands of a variant (RKF7(8) stage 12)
+constexpr int kOpsMax = 3 + 2 * kNkMax;    // shared-memory operand slots
+// Operand slots of variant V: the stage velocity, y_r, y_v, then nk K_r and nk K_v.
+struct Ops {
+    int nk, KV;
+    __device__ explicit Ops(int V) : nk(var_nk(V)), KV(3 + var_nk(V)) {}
+    static constexpr int VS = 0, YR = 1, YV = 2, KR = 3;
 };
+// Source stages of the RKF7(8) combinations (Tableau::src), for runtime indexing.
+static __constant__ int c_src[13][kNkMax] = {
+    {0}, {0}, {0, 1}, {0, 2}, {0, 2, 3}, {0, 3, 4}, {0, 3, 4, 5}, {0, 4, 5, 6},
+    {0, 3, 4, 5, 6, 7}, {0, 3, 4, 5, 6, 7, 8}, {0, 3, 4, 5, 6, 7, 8, 9},
+    {0, 5, 6, 7, 8, 9}, {0, 3, 4, 5, 6, 7, 8, 9, 11}};
 // Stage index of operand q of variant V.
-template <int V> __device__ __forceinline__ int op_src(int q)
+__device__ __forceinline__ int op_src(int V, int q)
 {
-    if constexpr (V >= 1 && V <= 12) return kSrc[V][q];
-    else if constexpr (V == 14) return q;
-    else if constexpr (V == 15) return q == 0 ? 0 : (q == 1 ? 10 : 11);
-    else return 3;
+    if (V >= 1 && V <= 12) return c_src[V][q];
+    if (V == 14) return q;
+    if (V == 15) return q == 0 ? 0 : (q == 1 ? 10 : 11);
+    return 3;
 }
 
 // Gravity of the chunk's sources on SPT sinks per thread, FP32 modes.  The
@@ -342,14 +352,14 @@ __device__ __forceinline__ void gravity_f64(SmemStage& sm, const StageParams& P,
 // memory by cp.async at the start, so they arrive during the gravity loop
 // without holding registers.
 // ---------------------------------------------------------------------------
-template <int MODE, bool EXACT, int V>
-__global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
+template <int MODE, bool EXACT>
+__global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const int V)
 {
     constexpr bool kF32 = (MODE == MODE_MIXED || MODE == MODE_FP32);
-    constexpr bool kRkf = (V >= 1 && V <= 12);
-    using O = Ops<V>;
+    const bool kRkf = (V >= 1 && V <= 12);
+    const Ops O(V);
     __shared__ SmemStage sm;
-    __shared__ double ops[O::N][kMaxElem];
+    __shared__ double ops[kOpsMax][kMaxElem];
     const GravItem it = P.items[blockIdx.x];
     const int s = P.stage;
     // Stage 0 follows the kernels that update the system records, y and the
@@ -382,15 +392,14 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
     const bool drag_on = P.gas.enabled && it.cls == CLS_NSI;
     const bool need_vs = drag_on || V != 0;
     if (elem) {   // copy group 0: the operands older than the previous stage
-        if constexpr (V >= 1 && V <= 14) {
-            cp_async8(&ops[O::YR][t], P.y_r + x);
-            cp_async8(&ops[O::YV][t], P.y_v + x);
+        if (V >= 1 && V <= 14) {
+            cp_async8(&ops[O.YR][t], P.y_r + x);
+            cp_async8(&ops[O.YV][t], P.y_v + x);
         }
-#pragma unroll
-        for (int q = 0; q < O::nk; q++) {
-            const int src = op_src<V>(q);
-            if (src != s) cp_async8(&ops[O::KR + q][t], P.Kr[src] + x);
-            if (!(kRkf && src == V - 1) && src != s - 1) cp_async8(&ops[O::KV + q][t], P.Kv[src] + x);
+        for (int q = 0; q < O.nk; q++) {
+            const int src = op_src(V, q);
+            if (src != s) cp_async8(&ops[O.KR + q][t], P.Kr[src] + x);
+            if (!(kRkf && src == V - 1) && src != s - 1) cp_async8(&ops[O.KV + q][t], P.Kv[src] + x);
         }
     }
     cp_async_commit();
@@ -451,12 +460,11 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
     }
     cp_async_commit();
     if (elem) {   // copy group B: the operands the previous stage wrote
-        if (need_vs) cp_async8(&ops[O::VS][t], P.Kr[s] + x);
-#pragma unroll
-        for (int q = 0; q < O::nk; q++) {
-            const int src = op_src<V>(q);
-            if (src == s) cp_async8(&ops[O::KR + q][t], P.Kr[src] + x);
-            if (!(kRkf && src == V - 1) && src == s - 1) cp_async8(&ops[O::KV + q][t], P.Kv[src] + x);
+        if (need_vs) cp_async8(&ops[O.VS][t], P.Kr[s] + x);
+        for (int q = 0; q < O.nk; q++) {
+            const int src = op_src(V, q);
+            if (src == s) cp_async8(&ops[O.KR + q][t], P.Kr[src] + x);
+            if (!(kRkf && src == V - 1) && src == s - 1) cp_async8(&ops[O.KV + q][t], P.Kv[src] + x);
         }
     }
     cp_async_commit();
@@ -587,7 +595,7 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
     if (!elem) return;
 
     // ---- element-wise FP64 epilogue ----
-    const double vs = need_vs ? ops[O::VS][t] : 0.0;   // stage velocity of the element
+    const double vs = need_vs ? ops[O.VS][t] : 0.0;   // stage velocity of the element
     if (!(idi > 0)) a = 0.0;   // calc_grav_accel_naive zeroes inactive sinks (pp_disk.cu:386-388)
     if (drag_act) {
         const double g = ce == 0 ? sm.sc[ke][1] : (ce == 1 ? sm.sc[ke][2] : 0.0);
@@ -595,26 +603,27 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
     }
     P.Kv[s][x] = a;
 
-    if constexpr (V >= 1 && V <= 14) {
-        const double yr = ops[O::YR][t], yv = ops[O::YV][t];
+    if (V >= 1 && V <= 14) {
+        const double yr = ops[O.YR][t], yv = ops[O.YV][t];
         double orr, ovv;
-        if constexpr (kRkf) {
+        if (kRkf) {
             // ytemp of stage V: y + dt * sum_q a_{V,q} K_q, terms in red's order
             // (rk8_kernel::calc_ytemp_for_f1..f12, int_rungekutta8.cu:80-246)
-            constexpr int off = 1 + V * (V - 1) / 2;
-            const double kv0 = (kSrc[V][0] == V - 1) ? a : ops[O::KV][t];
-            double ar = mul<EXACT>(c_tb.a[off + kSrc[V][0]], ops[O::KR][t]);
-            double av = mul<EXACT>(c_tb.a[off + kSrc[V][0]], kv0);
-#pragma unroll
-            for (int q = 1; q < O::nk; q++) {
-                const double aq = c_tb.a[off + kSrc[V][q]];
-                const double kvq = (kSrc[V][q] == V - 1) ? a : ops[O::KV + q][t];
-                ar = madd<EXACT>(ar, aq, ops[O::KR + q][t]);
+            const int off = 1 + V * (V - 1) / 2;
+            const int s0 = c_src[V][0];
+            const double kv0 = (s0 == V - 1) ? a : ops[O.KV][t];
+            double ar = mul<EXACT>(c_tb.a[off + s0], ops[O.KR][t]);
+            double av = mul<EXACT>(c_tb.a[off + s0], kv0);
+            for (int q = 1; q < O.nk; q++) {
+                const int sq = c_src[V][q];
+                const double aq = c_tb.a[off + sq];
+                const double kvq = (sq == V - 1) ? a : ops[O.KV + q][t];
+                ar = madd<EXACT>(ar, aq, ops[O.KR + q][t]);
                 av = madd<EXACT>(av, aq, kvq);
             }
             orr = madd<EXACT>(yr, dt, ar);
             ovv = madd<EXACT>(yv, dt, av);
-        } else if constexpr (V == 13) {
+        } else if (V == 13) {
             // rk4_kernel::sum_vector, int_rungekutta4.cu:36-47: y + (a dt) K_s
             const double bf = mul<EXACT>(c_tb.a4[s + 1], dt);
             orr = madd<EXACT>(yr, bf, vs);
@@ -622,24 +631,24 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
         } else {
             // RK4 y_{n+1} as the positions of the adaptive stage 4
             const double b0 = mul<EXACT>(c_tb.b4[0], dt), b1 = mul<EXACT>(c_tb.b4[1], dt);
-            orr = rk4_ynp1<EXACT>(yr, b0, b1, ops[O::KR][t], ops[O::KR + 1][t], ops[O::KR + 2][t], vs);
-            ovv = rk4_ynp1<EXACT>(yv, b0, b1, ops[O::KV][t], ops[O::KV + 1][t], ops[O::KV + 2][t], a);
+            orr = rk4_ynp1<EXACT>(yr, b0, b1, ops[O.KR][t], ops[O.KR + 1][t], ops[O.KR + 2][t], vs);
+            ovv = rk4_ynp1<EXACT>(yv, b0, b1, ops[O.KV][t], ops[O.KV + 1][t], ops[O.KV + 2][t], a);
         }
         P.r_out[x] = orr;
         P.Kr[P.next][x] = ovv;
         write_pos_c(P.pos_hi_out, P.pos_lo_out, ie, ce, orr);   // x, y, z; k_prep holds the .w words
-    } else if constexpr (V == 15 || V == 16) {
+    } else if (V == 15 || V == 16) {
         double e = 0.0;
         if (ie - it.soff < it.nerr) {
             double er, ev;
-            if constexpr (V == 15) {
+            if (V == 15) {
                 // rk8_kernel::calc_error, int_rungekutta8.cu:248-260
-                er = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(ops[O::KR][t], ops[O::KR + 1][t]), ops[O::KR + 2][t]), vs));
-                ev = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(ops[O::KV][t], ops[O::KV + 1][t]), ops[O::KV + 2][t]), a));
+                er = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(ops[O.KR][t], ops[O.KR + 1][t]), ops[O.KR + 2][t]), vs));
+                ev = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(ops[O.KV][t], ops[O.KV + 1][t]), ops[O.KV + 2][t]), a));
             } else {
                 // rk4_kernel::calc_error, int_rungekutta4.cu:62-73
-                er = fabs(ops[O::KR][t] - vs);
-                ev = fabs(ops[O::KV][t] - a);
+                er = fabs(ops[O.KR][t] - vs);
+                ev = fabs(ops[O.KV][t] - a);
             }
             e = fmax(er, ev);
             if (er != er || ev != ev) e = __longlong_as_double(0x7ff8000000000000ll);
@@ -659,29 +668,12 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P)
     }
 }
 
-// Launches the variant of k_stage that P asks for (stage_variant).
+// Launches k_stage for variant v (stage_variant): one kernel per mode serves
+// every stage of a try, so its code stays in the caches from stage to stage.
 template <int MODE, bool EXACT>
 void launch_stage_variant(const StageParams& P, int n, int v, cudaStream_t s)
 {
-    switch (v) {
-    case 1: launch_k(k_stage<MODE, EXACT, 1>, n, kTile, s, P); break;
-    case 2: launch_k(k_stage<MODE, EXACT, 2>, n, kTile, s, P); break;
-    case 3: launch_k(k_stage<MODE, EXACT, 3>, n, kTile, s, P); break;
-    case 4: launch_k(k_stage<MODE, EXACT, 4>, n, kTile, s, P); break;
-    case 5: launch_k(k_stage<MODE, EXACT, 5>, n, kTile, s, P); break;
-    case 6: launch_k(k_stage<MODE, EXACT, 6>, n, kTile, s, P); break;
-    case 7: launch_k(k_stage<MODE, EXACT, 7>, n, kTile, s, P); break;
-    case 8: launch_k(k_stage<MODE, EXACT, 8>, n, kTile, s, P); break;
-    case 9: launch_k(k_stage<MODE, EXACT, 9>, n, kTile, s, P); break;
-    case 10: launch_k(k_stage<MODE, EXACT, 10>, n, kTile, s, P); break;
-    case 11: launch_k(k_stage<MODE, EXACT, 11>, n, kTile, s, P); break;
-    case 12: launch_k(k_stage<MODE, EXACT, 12>, n, kTile, s, P); break;
-    case 13: launch_k(k_stage<MODE, EXACT, 13>, n, kTile, s, P); break;
-    case 14: launch_k(k_stage<MODE, EXACT, 14>, n, kTile, s, P); break;
-    case 15: launch_k(k_stage<MODE, EXACT, 15>, n, kTile, s, P); break;
-    case 16: launch_k(k_stage<MODE, EXACT, 16>, n, kTile, s, P); break;
-    default: launch_k(k_stage<MODE, EXACT, 0>, n, kTile, s, P); break;
-    }
+    launch_k(k_stage<MODE, EXACT>, (unsigned)n, (unsigned)kTile, s, P, v);
 }
 
 }  // namespace redgb
