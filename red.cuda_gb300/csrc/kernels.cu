@@ -3,8 +3,11 @@
 //   (k_stage, one Runge-Kutta stage, is in stage.cuh / stage_*.cu)
 //   k_prep      positions of stage 0 from y (FP32 double-single copies)
 //   k_control   per-system error -> accept / reject -> new step size
-//   k_finish    y_{n+1} for accepted systems, positions of the next stage 0
-//   k_collision pairwise overlap test, FP32 prefilter + red's FP64 test
+//   k_finish    y_{n+1} for accepted systems, positions of the next stage 0,
+//               the small bodies into the collision check's spatial hash
+//   k_collide   the collision check after a try: tile pairs of the large
+//               bodies (FP32 prefilter + red's FP64 test) and hash queries
+//   k_collision, k_grid_insert, k_grid_query   the same, for the explicit check
 //   k_ejhc      ejection / hit-centrum test
 //   k_potential per-body potential sums for the integrals
 #include <cfloat>
@@ -91,6 +94,35 @@ __global__ void k_control(const ControlParams P)
     if (P.length != 0.0 && fabs(S.t - S.t_start) > fabs(P.length)) S.active = 0;
 }
 
+// Spatial-hash broad phase for the small bodies.  Cell coordinates are
+// clamped so that far-away bodies share border cells (tested exactly, never
+// missed).
+__device__ __forceinline__ int4 cell_of(double x, double y, double z, double inv_h)
+{
+    const double lim = 1.0e9;
+    int4 c;
+    c.x = (int)floor(fmin(fmax(x * inv_h, -lim), lim));
+    c.y = (int)floor(fmin(fmax(y * inv_h, -lim), lim));
+    c.z = (int)floor(fmin(fmax(z * inv_h, -lim), lim));
+    c.w = 0;
+    return c;
+}
+
+__device__ __forceinline__ int bucket_of(int cx, int cy, int cz, int mask)
+{
+    const unsigned h = ((unsigned)cx * 73856093u) ^ ((unsigned)cy * 19349663u) ^ ((unsigned)cz * 83492791u);
+    return (int)(h & (unsigned)mask);
+}
+
+// Inserts small body i at position (x, y, z) into its system's hash table.
+__device__ __forceinline__ void grid_insert_one(const GridInfo& g, int4* cell, int* next, int* head, int i, double x,
+                                                double y, double z)
+{
+    const int4 c = cell_of(x, y, z, g.inv_h);
+    cell[i] = c;
+    next[i] = atomicExch(&head[g.toff + bucket_of(c.x, c.y, c.z, g.mask)], i);
+}
+
 // y_{n+1} of the accepted systems and the positions of the next stage 0.  Four
 // threads per body: lanes 0..2 the x, y, z components, lane 3 the mass / radius
 // words of the FP32 copies.  Segments of kFinishBodies bodies.
@@ -99,22 +131,20 @@ __global__ void __launch_bounds__(4 * kFinishBodies) k_finish(const FinishParams
 {
     pdl_wait();
     pdl_trigger();
-    if (P.head) {   // the spatial hash of the collision check that follows starts empty
-        const long long nt = (long long)gridDim.x * blockDim.x;
-        for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < P.head_n; k += nt) P.head[k] = -1;
-    }
     const Segment sg = P.segs[blockIdx.x];
     DevSys* S = P.sys + sg.sys;
     if (S->halted) return;
     const int i = sg.b0 + threadIdx.x / 4;
     const int c = threadIdx.x % 4;
     const bool acc = S->accepted;
-    if (!acc && !runnable(*S)) return;
-    if (i >= sg.b1) return;
-    if (c == 3) return;   // the .w words (mass, radius) are set by k_prep
-    const int x = 3 * i + c;
-    double r;
-    if (acc) {
+    if (!acc && !runnable(*S)) return;   // uniform over the CTA
+    if (i >= sg.b1) return;              // uniform over the body's four lanes
+    // lane 3 holds no component (the .w words, mass and radius, are set by
+    // k_prep); it inserts the body into the collision check's spatial hash
+    const int x = 3 * i + min(c, 2);
+    double r = 0.0;
+    if (c == 3) {
+    } else if (acc) {
         const double dt = S->dt_did;
         double v;
         if (P.scheme == SCHEME_RKF78) {
@@ -135,6 +165,14 @@ __global__ void __launch_bounds__(4 * kFinishBodies) k_finish(const FinishParams
         r = P.y_r[x];
     }
     write_pos_c(P.pos_hi0, P.pos_lo0, i, c, r);
+    if (P.head && acc) {
+        const int l0 = (int)(threadIdx.x & 31u) & ~3;
+        const unsigned gm = 0xFu << l0;   // the body's four lanes
+        const double rx = __shfl_sync(gm, r, l0), ry = __shfl_sync(gm, r, l0 + 1), rz = __shfl_sync(gm, r, l0 + 2);
+        const GridInfo g = P.grid[sg.sys];
+        if (c == 3 && g.enabled && i >= P.sinfo[sg.sys].off + P.sinfo[sg.sys].n_SI)
+            grid_insert_one(g, P.cell, P.next, P.head, i, rx, ry, rz);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -188,12 +226,10 @@ __device__ __forceinline__ void collide_exact(const CollParams& P, DevSys* S, in
 // One thread per later body j; the i tile (the SI bodies) sits in shared
 // memory.  FP32 double-single prefilter with a safety margin, red's FP64
 // test decides.
-__global__ void __launch_bounds__(kTile) k_collision(const CollParams P)
+__device__ __forceinline__ void coll_pairs(const CollParams& P, int item)
 {
     __shared__ float4 shi[kTile], slo[kTile];
-    pdl_wait();
-    pdl_trigger();
-    const PairItem it = P.items[blockIdx.x];
+    const PairItem it = P.items[item];
     DevSys* S = P.sys + it.sys;
     if (!coll_runs(P, *S)) return;
     const SysInfo si = P.sinfo[it.sys];
@@ -222,25 +258,14 @@ __global__ void __launch_bounds__(kTile) k_collision(const CollParams P)
     }
 }
 
-// Spatial-hash broad phase for the small bodies.  Cell coordinates are
-// clamped so that far-away bodies share border cells (tested exactly, never
-// missed).
-__device__ __forceinline__ int4 cell_of(double x, double y, double z, double inv_h)
+__global__ void __launch_bounds__(kTile) k_collision(const CollParams P)
 {
-    const double lim = 1.0e9;
-    int4 c;
-    c.x = (int)floor(fmin(fmax(x * inv_h, -lim), lim));
-    c.y = (int)floor(fmin(fmax(y * inv_h, -lim), lim));
-    c.z = (int)floor(fmin(fmax(z * inv_h, -lim), lim));
-    c.w = 0;
-    return c;
+    pdl_wait();
+    pdl_trigger();
+    coll_pairs(P, blockIdx.x);
 }
 
-__device__ __forceinline__ int bucket_of(int cx, int cy, int cz, int mask)
-{
-    const unsigned h = ((unsigned)cx * 73856093u) ^ ((unsigned)cy * 19349663u) ^ ((unsigned)cz * 83492791u);
-    return (int)(h & (unsigned)mask);
-}
+
 
 __global__ void __launch_bounds__(kSegment) k_grid_insert(const CollParams P)
 {
@@ -253,9 +278,7 @@ __global__ void __launch_bounds__(kSegment) k_grid_insert(const CollParams P)
     const SysInfo si = P.sinfo[sg.sys];
     const int i = sg.b0 + threadIdx.x;
     if (i >= sg.b1 || i < si.off + si.n_SI) return;
-    const int4 c = cell_of(P.y_r[3 * i], P.y_r[3 * i + 1], P.y_r[3 * i + 2], g.inv_h);
-    P.cell[i] = c;
-    P.next[i] = atomicExch(&P.head[g.toff + bucket_of(c.x, c.y, c.z, g.mask)], i);
+    grid_insert_one(g, P.cell, P.next, P.head, i, P.y_r[3 * i], P.y_r[3 * i + 1], P.y_r[3 * i + 2]);
 }
 
 // Half of the neighbourhood: the own cell (pairs with j > i) and the 13 cells
@@ -264,16 +287,14 @@ __global__ void __launch_bounds__(kSegment) k_grid_insert(const CollParams P)
 // i < j loop.  The 14 bucket lists are walked side by side: each round loads
 // the current element of every list at once, so a thread needs as many
 // dependent memory round trips as its longest list, not their sum.
-__global__ void __launch_bounds__(kSegment) k_grid_query(const CollParams P)
+__device__ __forceinline__ void grid_query(const CollParams& P, int seg, int local)
 {
-    pdl_wait();
-    pdl_trigger();
-    const Segment sg = P.segs[blockIdx.x];
+    const Segment sg = P.segs[seg];
     DevSys* S = P.sys + sg.sys;
     const GridInfo g = P.grid[sg.sys];
     if (!g.enabled || !coll_runs(P, *S)) return;
     const SysInfo si = P.sinfo[sg.sys];
-    const int i = sg.b0 + threadIdx.x;
+    const int i = sg.b0 + local;
     if (i >= sg.b1 || i < si.off + si.n_SI) return;
     const double f = P.factor * P.factor;
     const int4 c = P.cell[i];
@@ -318,6 +339,29 @@ __global__ void __launch_bounds__(kSegment) k_grid_query(const CollParams P)
             }
         }
     }
+}
+
+__global__ void __launch_bounds__(kSegment) k_grid_query(const CollParams P)
+{
+    pdl_wait();
+    pdl_trigger();
+    grid_query(P, blockIdx.x, threadIdx.x);
+}
+
+// The collision check after a try in one launch: CTAs [0, n_pairs) test the
+// tile pairs of the large bodies, the others run the hash-grid query for half
+// a segment each (the bodies were inserted by k_finish).
+static_assert(kSegment == 2 * kTile, "k_collide runs half a segment per CTA");
+__global__ void __launch_bounds__(kTile) k_collide(const CollParams P, int n_pairs)
+{
+    pdl_wait();
+    pdl_trigger();
+    if ((int)blockIdx.x < n_pairs) {
+        coll_pairs(P, blockIdx.x);
+        return;
+    }
+    const int q = (int)blockIdx.x - n_pairs;
+    grid_query(P, q / 2, (q % 2) * kTile + (int)threadIdx.x);
 }
 
 // kernel_pp_disk::check_for_ejection_hit_centrum (pp_disk.cu:283-318)
@@ -506,16 +550,24 @@ void launch_finish(const FinishParams& P, int n_segs, cudaStream_t s)
     else launch_k(k_finish<false>, (unsigned)n_segs, 4u * kFinishBodies, s, P);
 }
 
-// head_cleared: the bucket heads were set to -1 by the preceding k_finish.
+// The explicit collision check (red_check_for_collision) on the current state.
 void launch_collision(const CollParams& P, int n_items, int n_segs, bool use_grid, size_t table_size,
-                      bool head_cleared, cudaStream_t s)
+                      cudaStream_t s)
 {
     if (n_items > 0) launch_k(k_collision, (unsigned)n_items, (unsigned)kTile, s, P);
     if (use_grid && n_segs > 0) {
-        if (!head_cleared) cudaMemsetAsync(P.head, 0xff, table_size * sizeof(int), s);
+        cudaMemsetAsync(P.head, 0xff, table_size * sizeof(int), s);
         launch_k(k_grid_insert, (unsigned)n_segs, (unsigned)kSegment, s, P);
         launch_k(k_grid_query, (unsigned)n_segs, (unsigned)kSegment, s, P);
     }
+}
+
+// The collision check after a try (k_collide): the bodies are in the hash
+// already (k_finish), the pair tiles and the queries run in one launch.
+void launch_collide(const CollParams& P, int n_items, int n_segs, bool use_grid, cudaStream_t s)
+{
+    const int nq = use_grid ? 2 * n_segs : 0;
+    if (n_items + nq > 0) launch_k(k_collide, (unsigned)(n_items + nq), (unsigned)kTile, s, P, n_items);
 }
 
 void launch_pack_state(int o, int n, const double* y_r, const double* y_v, const double* mass, const double* radius,

@@ -158,6 +158,8 @@ struct StageParams {
     double* partial;      // 3 doubles per record
     unsigned int* tile_cnt;
     GasDev gas;
+    int* head;            // stage 0 sets the collision check's bucket heads to -1 (not null)
+    long long head_n;
 };
 
 struct FinishParams {
@@ -177,8 +179,12 @@ struct FinishParams {
     const int* id;
     float4* pos_hi0;
     float4* pos_lo0;
-    int* head;                // spatial-hash bucket heads, set to -1 here when not null
-    long long head_n;
+    // spatial hash of the collision check that follows (head not null): the
+    // accepted systems' small bodies are inserted at their new positions
+    int* head;
+    int* next;
+    int4* cell;
+    const GridInfo* grid;
 };
 
 struct ControlParams {
@@ -265,7 +271,8 @@ void launch_prep(const Segment* segs, int n_segs, const SysInfo* sinfo, const De
 void launch_control(const ControlParams& P, cudaStream_t s);
 void launch_finish(const FinishParams& P, int n_segs, cudaStream_t s);
 void launch_collision(const CollParams& P, int n_items, int n_segs, bool use_grid, size_t table_size,
-                      bool head_cleared, cudaStream_t s);
+                      cudaStream_t s);
+void launch_collide(const CollParams& P, int n_items, int n_segs, bool use_grid, cudaStream_t s);
 void launch_ejhc(const EjhcParams& P, int n_segs, cudaStream_t s);
 void launch_set_quota(DevSys* sys, int n_sys, int q, cudaStream_t s);
 void launch_pack_state(int o, int n, const double* y_r, const double* y_v, const double* mass, const double* radius,

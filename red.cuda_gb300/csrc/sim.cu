@@ -764,8 +764,14 @@ void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs
         evs->push_back(e);
     };
     mark(-1);
+    const bool coll = cfg.threshold[RED_THRESHOLD_RADII_ENHANCE_FACTOR] > 0.0;
+    const bool hash = coll && use_grid && !segs.empty();   // the small bodies' spatial hash
     for (int s = 0; s < n_stage; s++) {
         StageParams P = stage_params(s, false);
+        if (s == 0 && hash) {
+            P.head = d_head;
+            P.head_n = (long long)table_size;
+        }
         launch_stage(P, (int)items.size(), mode, stream);
         mark(0);
         n++;
@@ -805,10 +811,11 @@ void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs
     F.id = id;
     F.pos_hi0 = pos_hi[0];
     F.pos_lo0 = pos_lo[0];
-    const bool coll = cfg.threshold[RED_THRESHOLD_RADII_ENHANCE_FACTOR] > 0.0;
-    if (coll && use_grid && !segs.empty()) {
+    if (hash) {
         F.head = d_head;
-        F.head_n = (long long)table_size;
+        F.next = d_next;
+        F.cell = d_cell;
+        F.grid = d_grid;
     }
     launch_finish(F, (int)fsegs.size(), stream);
     mark(2);
@@ -820,9 +827,9 @@ void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs
         fill_coll(Q);
         Q.only_accepted = 1;
         Q.mark = 1;
-        launch_collision(Q, (int)pairs.size(), (int)segs.size(), use_grid, table_size, F.head != nullptr, stream);
+        launch_collide(Q, (int)pairs.size(), (int)segs.size(), hash, stream);
         mark(3);
-        n += (pairs.empty() ? 0 : 1) + (use_grid && !segs.empty() ? 2 : 0);
+        n += (!pairs.empty() || hash) ? 1 : 0;
     }
     if (cfg.threshold[RED_THRESHOLD_EJECTION_DISTANCE] > 0.0 || cfg.threshold[RED_THRESHOLD_HIT_CENTRUM_DISTANCE] > 0.0) {
         EjhcParams E;
@@ -1350,7 +1357,7 @@ static int check_generic(red_sim* sim, int collision, red_event_t* out, uint32_t
         Q.only_accepted = 0;
         Q.mark = 0;
         sim->prep_positions();
-        launch_collision(Q, (int)sim->pairs.size(), (int)sim->segs.size(), sim->use_grid, sim->table_size, false,
+        launch_collision(Q, (int)sim->pairs.size(), (int)sim->segs.size(), sim->use_grid, sim->table_size,
                          sim->stream);
     } else {
         EjhcParams E;

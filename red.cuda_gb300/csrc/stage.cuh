@@ -367,7 +367,13 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
     // only what the previous stage does not write: the system record (written
     // after the last stage), y, ids, masses, K_q of stages <= s - 2 (the stage
     // velocity Kr[q] is written by stage q - 1, the acceleration Kv[q] by q).
-    if (s == 0) pdl_wait();
+    if (s == 0) {
+        pdl_wait();
+        if (P.head) {   // the collision check at the end of this try starts from an empty hash
+            const long long nt = (long long)gridDim.x * blockDim.x;
+            for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < P.head_n; k += nt) P.head[k] = -1;
+        }
+    }
     DevSys* S = P.sys + it.sys;
     double tsys = 0.0, dt = 0.0;
     if (!P.standalone) {
