@@ -125,6 +125,7 @@ __device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_re
 // Operands of the epilogue of variant V, staged in shared memory by cp.async
 // at the start of the kernel: slot [slot][t] belongs to element thread t.
 constexpr int kMaxElem = 96;   // 3 * 32 sinks: the largest tile the planner makes
+static_assert(kMaxElem < kTile, "thread kTile - 1 holds no element of the epilogue");
 __host__ __device__ constexpr int var_nk(int v)
 {
     return v == 1 ? 1 : v == 2 ? 2 : v == 3 ? 2 : v == 4 ? 3 : v == 5 ? 3 : v == 6 ? 4 : v == 7 ? 4 : v == 8 ? 6
@@ -519,7 +520,9 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
     const int mine_c = (t % it.lanes) % 3;
 
     // ---- source chunks of one sink tile -> the CTA that finishes last sums them,
-    // every thread of it on a contiguous range of chunks, in a fixed order ----
+    // every thread of it on a contiguous range of chunks, in a fixed order.  The
+    // chunk counter is advanced by the last thread, which holds no element
+    // (3 nsink <= 96 < kTile), while the element threads form the star term ----
     float2 g_ds = make_float2(0.f, 0.f);   // gravity of the element, FP32 modes
     double a = 0.0;                         // gravity of the element, FP64 modes
     float2* acc2 = reinterpret_cast<float2*>(sm.acc);
@@ -530,13 +533,41 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
             else P.partial[rec] = mine;
         }
         __syncthreads();
-        if (t == 0) {
+        if (t == kTile - 1) {
             fence_acq_rel_gpu();   // release the CTA's partial record
             const unsigned prev = atomicAdd(&P.tile_cnt[it.tile], 1u);
             const bool last = prev == (unsigned)(it.nchunk - 1);
             if (last) fence_acq_rel_gpu();   // acquire the other chunks' records
             sm.flag = last;
         }
+    }
+
+    // ---- central-star term (FP32 modes), double-single: m_j d / |d|^3 per star,
+    // each element thread forming the factor of its own sink; a sum of its own,
+    // added to the gravity after the reduction ----
+    float2 star_ds = make_float2(0.f, 0.f);
+    if (star_term && elem) {
+        const float4 H = sm.snk.f.hi[ke], Lo = sm.snk.f.lo[ke];
+        auto star_one = [&](float4 S, float4 SL, float2 m) {
+            const float2 dx = dsn_sub(dsn(S.x, SL.x), dsn(H.x, Lo.x));
+            const float2 dy = dsn_sub(dsn(S.y, SL.y), dsn(H.y, Lo.y));
+            const float2 dz = dsn_sub(dsn(S.z, SL.z), dsn(H.z, Lo.z));
+            const float2 r2 = dsn_add(dsn_add(dsn_sqr(dx), dsn_sqr(dy)), dsn_sqr(dz));
+            const float2 ri = dsn_rsqrt(r2);
+            const float2 f = dsn_mul(m, dsn_mul(dsn_sqr(ri), ri));
+            star_ds = dsn_add(star_ds, dsn_mul(f, ce == 0 ? dx : (ce == 1 ? dy : dz)));
+        };
+        for (int q = 0; q < nst0; q++)
+            if (it.soff + q != ie) star_one(sm.star_hi[q], sm.star_lo[q], sm.star_m[q]);
+        for (int j = it.soff + kStarBatch; j < it.soff + it.nstar; j++) {   // more than kStarBatch stars
+            if (j == ie) continue;
+            const double m = P.id[j] < 0 ? 0.0 : P.mass[j];
+            const float mh = __double2float_rn(m);
+            star_one(P.pos_hi_in[j], P.pos_lo_in[j], make_float2(mh, __double2float_rn(m - (double)mh)));
+        }
+    }
+
+    if (it.nchunk > 1) {
         __syncthreads();
         if (!sm.flag) {        // uniform
             cp_async_wait_all();   // no copy may land in shared memory after the CTA has gone
@@ -572,30 +603,7 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
             else a = sm.acc[t];
         }
     }
-
-    // ---- central-star term (FP32 modes), double-single: m_j d / |d|^3 per star,
-    // each element thread forming the factor of its own sink ----
-    if (star_term && elem) {
-        const float4 H = sm.snk.f.hi[ke], Lo = sm.snk.f.lo[ke];
-        auto star_one = [&](float4 S, float4 SL, float2 m) {
-            const float2 dx = dsn_sub(dsn(S.x, SL.x), dsn(H.x, Lo.x));
-            const float2 dy = dsn_sub(dsn(S.y, SL.y), dsn(H.y, Lo.y));
-            const float2 dz = dsn_sub(dsn(S.z, SL.z), dsn(H.z, Lo.z));
-            const float2 r2 = dsn_add(dsn_add(dsn_sqr(dx), dsn_sqr(dy)), dsn_sqr(dz));
-            const float2 ri = dsn_rsqrt(r2);
-            const float2 f = dsn_mul(m, dsn_mul(dsn_sqr(ri), ri));
-            g_ds = dsn_add(g_ds, dsn_mul(f, ce == 0 ? dx : (ce == 1 ? dy : dz)));
-        };
-        for (int q = 0; q < nst0; q++)
-            if (it.soff + q != ie) star_one(sm.star_hi[q], sm.star_lo[q], sm.star_m[q]);
-        for (int j = it.soff + kStarBatch; j < it.soff + it.nstar; j++) {   // more than kStarBatch stars
-            if (j == ie) continue;
-            const double m = P.id[j] < 0 ? 0.0 : P.mass[j];
-            const float mh = __double2float_rn(m);
-            star_one(P.pos_hi_in[j], P.pos_lo_in[j], make_float2(mh, __double2float_rn(m - (double)mh)));
-        }
-    }
-    if (kF32) a = dsn_to_double(g_ds);
+    if (kF32) a = dsn_to_double(dsn_add(g_ds, star_ds));
 
     cp_async_wait_all();
     if (!elem) return;
