@@ -32,22 +32,40 @@ constexpr float kEps2 = 1.0e-24f;
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
 
-// Launches kernel k with the programmatic-stream-serialization attribute while
-// pdl_on() holds on this thread, as a plain launch otherwise.
+// Launches kernel k in thread-block clusters of `cluster` CTAs when cluster >
+// 1, and with the programmatic-stream-serialization attribute while pdl_on()
+// holds on this thread.
 template <typename... KArgs, typename... Args>
-inline void launch_k(void (*k)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args&&... args)
+inline void launch_kx(void (*k)(KArgs...), unsigned grid, unsigned block, unsigned cluster, cudaStream_t s,
+                      Args&&... args)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(block);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchAttribute at[2];
+    int na = 0;
+    if (pdl_on()) {
+        at[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[na].val.programmaticStreamSerializationAllowed = 1;
+        na++;
+    }
+    if (cluster > 1) {
+        at[na].id = cudaLaunchAttributeClusterDimension;
+        at[na].val.clusterDim.x = cluster;
+        at[na].val.clusterDim.y = 1;
+        at[na].val.clusterDim.z = 1;
+        na++;
+    }
     cfg.attrs = at;
-    cfg.numAttrs = pdl_on() ? 1 : 0;
+    cfg.numAttrs = na;
     cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
+template <typename... KArgs, typename... Args>
+inline void launch_k(void (*k)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args&&... args)
+{
+    launch_kx(k, grid, block, 1u, s, std::forward<Args>(args)...);
 }
 
 // ---------------------------------------------------------------------------

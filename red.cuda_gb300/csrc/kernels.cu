@@ -531,6 +531,13 @@ void launch_stage(const StageParams& P, int n_items, int mode, cudaStream_t s)
     }
 }
 
+int stage_active_clusters(int mode)
+{
+    if (mode == MODE_MIXED) return active_clusters_mixed();
+    if (mode == MODE_FP32) return active_clusters_fp32();
+    return 0;
+}
+
 void launch_prep(const Segment* segs, int n_segs, const SysInfo* sinfo, const DevSys* sys, const double* y_r,
                  const double* mass, const double* radius, const int* id, float4* hi, float4* lo, float4* hi1,
                  float4* lo1, int all, cudaStream_t s)

@@ -20,6 +20,7 @@ namespace redgb {
 constexpr int kTile = 128;          // sinks per CTA and sources per shared-memory tile
 constexpr int kSegment = 256;       // bodies per CTA in the per-body kernels
 constexpr int kFinishBodies = 64;   // bodies per CTA of k_finish (four threads each)
+constexpr int kClusterChunks = 16;  // source chunks of a tile in a cluster launch (one cluster)
 constexpr int kMaxStages = 13;
 
 enum Mode { MODE_MIXED = 0, MODE_FP64 = 1, MODE_FP64_EXACT = 2, MODE_FP32 = 3 };
@@ -160,6 +161,7 @@ struct StageParams {
     GasDev gas;
     int* head;            // stage 0 sets the collision check's bucket heads to -1 (not null)
     long long head_n;
+    int cluster;          // 1: launched in clusters of kClusterChunks CTAs (items laid out for it)
 };
 
 struct FinishParams {
@@ -262,6 +264,11 @@ void set_tableau_fp32(const Tableau& tb, cudaStream_t s);
 void set_tableau_fp64(const Tableau& tb, cudaStream_t s);
 void set_tableau_exact(const Tableau& tb, cudaStream_t s);
 void launch_stage_mixed(const StageParams& P, int n, int variant, cudaStream_t s);
+// Clusters of kClusterChunks stage CTAs resident at once (FP32 modes; 0 for
+// the others or when the query fails).
+int active_clusters_mixed();
+int active_clusters_fp32();
+int stage_active_clusters(int mode);
 void launch_stage_fp32(const StageParams& P, int n, int variant, cudaStream_t s);
 void launch_stage_fp64(const StageParams& P, int n, int variant, cudaStream_t s);
 void launch_stage_exact(const StageParams& P, int n, int variant, cudaStream_t s);

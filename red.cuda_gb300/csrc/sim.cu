@@ -269,6 +269,76 @@ void plan_gravity_items(const SysInfo& si, int s, int mode, int chunk_override, 
         }
     }
 }
+// Items of a cluster launch (FP32 modes): a tile whose source list is longer
+// than two tiles becomes kClusterChunks chunks, the CTAs of one cluster; the
+// others are single items.  max_chunk is the longest chunk.
+static void plan_cluster_items(const SysInfo& si, int s, int mode, int lanes_cap, const double* star_mass,
+                               std::vector<GravItem>& groups, std::vector<GravItem>& singles, int& max_chunk)
+{
+    GravClass cls[3];
+    gravity_classes(si, mode, cls);
+    for (const GravClass& q : cls) {
+        const int nsink_all = q.s1 - q.s0;
+        if (nsink_all <= 0) continue;
+        const int nsrc = std::max(0, q.j1 - q.j0);
+        int lanes, spt;
+        class_shape(mode, nsink_all, nsrc, lanes_cap, lanes, spt);
+        const int tile_sinks = kTile / lanes * spt;
+        const int ntile = (nsink_all + tile_sinks - 1) / tile_sinks;
+        const int nchunk = nsrc > 2 * kTile ? kClusterChunks : 1;
+        const int chunk = std::max(1, (nsrc + nchunk - 1) / nchunk);
+        max_chunk = std::max(max_chunk, chunk);
+        for (int t = 0; t < ntile; t++) {
+            const int s0 = q.s0 + t * tile_sinks;
+            GravItem g;
+            memset(&g, 0, sizeof(g));
+            g.sys = s;
+            g.sink0 = si.off + s0;
+            g.nsink = std::min(tile_sinks, q.s1 - s0);
+            g.nchunk = nchunk;
+            g.lanes = lanes;
+            g.spt = spt;
+            g.cls = q.cls;
+            g.soff = si.off;
+            g.nstar = si.n_star;
+            g.nerr = si.n_err;
+            if (star_mass && si.n_star > 0) {
+                g.mstar_set = 1;
+                g.mstar_hi = (float)*star_mass;
+                g.mstar_lo = (float)(*star_mass - (double)g.mstar_hi);
+            }
+            g.tile = -1;
+            for (int c = 0; c < nchunk; c++) {
+                g.chunk = c;
+                g.src0 = si.off + q.j0 + std::min(nsrc, c * chunk);
+                g.src1 = si.off + q.j0 + std::min(nsrc, (c + 1) * chunk);
+                (nchunk > 1 ? groups : singles).push_back(g);
+            }
+        }
+    }
+}
+
+// The layout a cluster launch relies on: every chunked tile fills exactly one
+// cluster (chunks 0 .. kClusterChunks - 1 at ranks 0 .. kClusterChunks - 1, one
+// system), the other clusters hold single items (or padding, nsink = 0), and
+// the item count is a multiple of the cluster size.
+static void check_cluster_layout(const std::vector<GravItem>& items)
+{
+    if (items.size() % kClusterChunks) throw ArgError{RED_ERR_ARG, "internal error, cluster plan: ragged item count"};
+    for (size_t b = 0; b < items.size(); b += kClusterChunks) {
+        const GravItem& g0 = items[b];
+        for (int r = 0; r < kClusterChunks; r++) {
+            const GravItem& g = items[b + r];
+            if (g0.nchunk > 1) {
+                if (g.nchunk != kClusterChunks || g.chunk != r || g.sys != g0.sys || g.sink0 != g0.sink0 ||
+                    g.nsink <= 0)
+                    throw ArgError{RED_ERR_ARG, "internal error, cluster plan: a chunk group is split"};
+            } else if (g.nchunk != 1) {
+                throw ArgError{RED_ERR_ARG, "internal error, cluster plan: a chunk group is misaligned"};
+            }
+        }
+    }
+}
 }  // namespace redgb
 
 struct red_sim {
@@ -351,6 +421,7 @@ struct red_sim {
     std::vector<SysInfo> sinfo;
     std::vector<GridInfo> grid;
     int chunk_override = 0;     // sources per chunk chosen by the autotuner (0 = heuristic)
+    bool use_cluster = false;   // the plan's items are laid out for a cluster launch
     int lanes_cap = 32;         // upper bound on threads per sink (autotuner)
 
     cudaGraphExec_t graph = nullptr;
@@ -638,6 +709,34 @@ void red_sim::build_plan()
             table += m;
         }
     }
+    // Cluster plan (FP32 modes): when every tile's chunks fit the two-tile
+    // shared-memory buffer as kClusterChunks chunks and the whole launch, laid
+    // out in clusters, is resident at once, a tile's chunks run as the CTAs of
+    // one thread-block cluster and reduce through distributed shared memory:
+    // no GPU-scope fence or global partial records on the critical path.
+    // REDGB_CLUSTER=0 keeps the global reduction.
+    use_cluster = false;
+    const char* cenv = getenv("REDGB_CLUSTER");
+    if ((mode == MODE_MIXED || mode == MODE_FP32) && chunk_override == 0 && !(cenv && cenv[0] == '0')) {
+        std::vector<GravItem> groups, singles;
+        int max_chunk = 0;
+        for (uint32_t s = 0; s < n_sys; s++)
+            plan_cluster_items(sinfo[s], (int)s, mode, lanes_cap, &star_mass[s], groups, singles, max_chunk);
+        if (!groups.empty() && max_chunk <= 2 * kTile) {
+            GravItem pad;   // padding: nsink = 0, the CTA returns at once
+            memset(&pad, 0, sizeof(pad));
+            pad.nchunk = 1;
+            pad.tile = -1;
+            std::vector<GravItem> cl(groups);
+            cl.insert(cl.end(), singles.begin(), singles.end());
+            while (cl.size() % kClusterChunks) cl.push_back(pad);
+            if ((int)(cl.size() / kClusterChunks) <= stage_active_clusters(mode)) {
+                check_cluster_layout(cl);
+                items.swap(cl);
+                use_cluster = true;
+            }
+        }
+    }
     auto upload = [&](auto& vec, auto*& dptr, size_t& cap) {
         using T = typename std::remove_reference<decltype(vec)>::type::value_type;
         if (vec.size() > cap) {
@@ -728,6 +827,7 @@ StageParams red_sim::stage_params(int s, bool standalone)
     P.mass = mass; P.radius = radius; P.density = density; P.cd = cd; P.id = id;
     P.partial = partial;
     P.tile_cnt = tile_cnt;
+    P.cluster = use_cluster ? 1 : 0;
     P.gas.enabled = cfg.gas_disk == 1;
     for (int k = 0; k < 2; k++) {
         P.gas.rho[k] = cfg.gas.rho[k];

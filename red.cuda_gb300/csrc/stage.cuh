@@ -133,6 +133,20 @@ __host__ __device__ constexpr int var_nk(int v)
 }
 constexpr int kNkMax = 9;                  // the most K operands of a variant (RKF7(8) stage 12)
 constexpr int kOpsMax = 3 + 2 * kNkMax;    // shared-memory operand slots
+// Thread-block cluster helpers (a tile's source chunks as one cluster): the
+// barrier in two halves (every thread of every CTA of the cluster arrives;
+// release / acquire at cluster scope) and a read of another CTA's shared memory.
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release;\n" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire;\n" ::: "memory"); }
+__device__ __forceinline__ float2 ld_cluster_f2(const float2* local, unsigned rank)
+{
+    unsigned a = (unsigned)__cvta_generic_to_shared(local), r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(a), "r"(rank));
+    float2 v;
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];\n" : "=f"(v.x), "=f"(v.y) : "r"(r) : "memory");
+    return v;
+}
+
 // Operand slots of variant V: the stage velocity, y_r, y_v, then nk K_r and nk K_v.
 struct Ops {
     int nk, KV;
@@ -353,7 +367,9 @@ __device__ __forceinline__ void gravity_f64(SmemStage& sm, const StageParams& P,
 // memory by cp.async at the start, so they arrive during the gravity loop
 // without holding registers.
 // ---------------------------------------------------------------------------
-template <int MODE, bool EXACT>
+// CL: the cluster-launch instance (FP32 modes), whose items are laid out in
+// clusters of kClusterChunks CTAs.
+template <int MODE, bool EXACT, bool CL>
 __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const int V)
 {
     constexpr bool kF32 = (MODE == MODE_MIXED || MODE == MODE_FP32);
@@ -374,6 +390,10 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
             const long long nt = (long long)gridDim.x * blockDim.x;
             for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < P.head_n; k += nt) P.head[k] = -1;
         }
+    }
+    if (CL && it.nsink == 0) {   // padding of the last cluster
+        pdl_wait();
+        return;
     }
     DevSys* S = P.sys + it.sys;
     double tsys = 0.0, dt = 0.0;
@@ -519,14 +539,22 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
     }
     const int mine_c = (t % it.lanes) % 3;
 
-    // ---- source chunks of one sink tile -> the CTA that finishes last sums them,
-    // every thread of it on a contiguous range of chunks, in a fixed order.  The
-    // chunk counter is advanced by the last thread, which holds no element
-    // (3 nsink <= 96 < kTile), while the element threads form the star term ----
+    // ---- source chunks of one sink tile.  In a cluster launch (FP32 modes) the
+    // tile's kClusterChunks chunks are the CTAs of one cluster: each leaves its
+    // partial in its shared memory and chunk 0 sums them through distributed
+    // shared memory, in chunk order.  Otherwise the CTA that finishes last sums
+    // the partial records in global memory, every thread of it on a contiguous
+    // range of chunks, in a fixed order; the chunk counter is advanced by the
+    // last thread, which holds no element (3 nsink <= 96 < kTile).  The element
+    // threads form the star term meanwhile ----
     float2 g_ds = make_float2(0.f, 0.f);   // gravity of the element, FP32 modes
     double a = 0.0;                         // gravity of the element, FP64 modes
     float2* acc2 = reinterpret_cast<float2*>(sm.acc);
-    if (it.nchunk > 1) {
+    const bool in_cluster = CL && it.nchunk > 1;   // uniform over the cluster
+    if (in_cluster) {
+        if (mine_ok) acc2[3 * mine_k + mine_c] = mine_ds;
+        cluster_arrive();
+    } else if (it.nchunk > 1) {
         if (mine_ok) {
             const long long rec = 3 * ((long long)it.part_off + (long long)it.chunk * it.nsink) + 3 * mine_k + mine_c;
             if (kF32) reinterpret_cast<float2*>(P.partial)[rec] = mine_ds;
@@ -567,7 +595,24 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
         }
     }
 
-    if (it.nchunk > 1) {
+    if (in_cluster) {
+        cluster_wait();   // every chunk's partial is in its CTA's shared memory
+        if (it.chunk == 0 && elem) {
+            for (int c0 = 0; c0 < kClusterChunks; c0 += 8) {   // loads in batches of 8, sums in chunk order
+                float2 v[8];
+#pragma unroll
+                for (int c = 0; c < 8; c++) v[c] = ld_cluster_f2(acc2 + t, (unsigned)(c0 + c));
+#pragma unroll
+                for (int c = 0; c < 8; c++) g_ds = dsn_add(g_ds, v[c]);
+            }
+        }
+        cluster_arrive();   // the other chunks keep their shared memory until chunk 0 has read it
+        cluster_wait();
+        if (it.chunk != 0) {
+            cp_async_wait_all();
+            return;
+        }
+    } else if (it.nchunk > 1) {
         __syncthreads();
         if (!sm.flag) {        // uniform
             cp_async_wait_all();   // no copy may land in shared memory after the CTA has gone
@@ -684,10 +729,53 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
 
 // Launches k_stage for variant v (stage_variant): one kernel per mode serves
 // every stage of a try, so its code stays in the caches from stage to stage.
+// Clusters of kClusterChunks CTAs are above the portable 8.
+template <int MODE, bool EXACT>
+void stage_attributes()
+{
+    static const bool done = [] {
+        cudaFuncSetAttribute(k_stage<MODE, EXACT, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        return true;
+    }();
+    (void)done;
+}
+
 template <int MODE, bool EXACT>
 void launch_stage_variant(const StageParams& P, int n, int v, cudaStream_t s)
 {
-    launch_k(k_stage<MODE, EXACT>, (unsigned)n, (unsigned)kTile, s, P, v);
+    if constexpr (MODE == MODE_MIXED || MODE == MODE_FP32) {
+        if (P.cluster) {
+            stage_attributes<MODE, EXACT>();
+            launch_kx(k_stage<MODE, EXACT, true>, (unsigned)n, (unsigned)kTile, (unsigned)kClusterChunks, s, P, v);
+            return;
+        }
+    }
+    launch_k(k_stage<MODE, EXACT, false>, (unsigned)n, (unsigned)kTile, s, P, v);
+}
+
+// Clusters of kClusterChunks stage CTAs that can be resident at once (FP32
+// modes; 0 if the query fails).
+template <int MODE, bool EXACT>
+int stage_active_clusters()
+{
+    stage_attributes<MODE, EXACT>();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kClusterChunks);
+    cfg.blockDim = dim3(kTile);
+    cfg.dynamicSmemBytes = 0;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = kClusterChunks;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k_stage<MODE, EXACT, true>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
 }
 
 }  // namespace redgb

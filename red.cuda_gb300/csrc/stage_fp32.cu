@@ -15,4 +15,6 @@ void launch_stage_fp32(const StageParams& P, int n, int variant, cudaStream_t s)
     launch_stage_variant<MODE_FP32, false>(P, n, variant, s);
 }
 
+int active_clusters_fp32() { return stage_active_clusters<MODE_FP32, false>(); }
+
 }  // namespace redgb

@@ -15,4 +15,6 @@ void launch_stage_mixed(const StageParams& P, int n, int variant, cudaStream_t s
     launch_stage_variant<MODE_MIXED, false>(P, n, variant, s);
 }
 
+int active_clusters_mixed() { return stage_active_clusters<MODE_MIXED, false>(); }
+
 }  // namespace redgb

@@ -67,6 +67,25 @@ def test_gravity_dense_mixed(rg, orc):
     assert err[1:].max() < 1e-8
 
 
+@pytest.mark.parametrize("cluster", ["1", "0"])
+def test_gravity_chunk_reduction_paths(rg, orc, monkeypatch, cluster):
+    """The large bodies' sums over more than two source tiles are split into
+    chunks: reduced through distributed shared memory within a thread-block
+    cluster (the default when the launch fits the GPU at once) or through
+    global partial records (REDGB_CLUSTER=0).  Both against the FP64 oracle
+    with the MIXED tolerances: 2e-6 for the star (FP32 pairs only), 2e-9 for
+    the bodies whose star term dominates."""
+    monkeypatch.setenv("REDGB_CLUSTER", cluster)
+    s = rg.ic.config2(seed=42, n_pp=8, n_pl=3000)
+    with rg.Sim(s, dt=0.01, precision="mixed") as sim:
+        a = vec(sim.calc_dydx(0, 1, 0.0))
+    _, ref = orc.grav_accel(obody(orc, s), sem=orc.SEM_GPU)
+    ref = vec(ref)
+    err = np.linalg.norm(a - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    assert err[0] < 2e-6
+    assert err[1:].max() < 2e-9, err[1:].max()
+
+
 def test_velocity_derivative(rg):
     s = small_disk(rg, n_pl=50)
     with rg.Sim(s, dt=0.01) as sim:

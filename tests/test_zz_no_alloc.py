@@ -9,8 +9,10 @@ a fresh process and after the other tests.
 The entry point is checked through the C ABI against the allocating entry
 point (red_calc_dydx with i = 1) on two calls in a row with different
 systems, so that nothing left in the shared array by the first call leaks
-into the second.  Tolerance: the same launch plan and summation order, so
-the results agree to 1e-12 relative (they are expected to be identical).
+into the second.  Tolerance: the same launch plan and summation order (the
+allocating side keeps the global chunk reduction, REDGB_CLUSTER=0, as the
+allocation-free entry point does), so the results agree to 1e-12 relative
+(they are expected to be identical).
 """
 import ctypes as C
 
@@ -53,8 +55,17 @@ def device_args(rg, torch, s, precision, t=0.0, gas=None):
 
 
 def reference(rg, s, precision, t=0.0, gas=None):
-    with rg.Sim(s, dt=0.01, precision=precision, gas=gas) as sim:
-        return vec(sim.calc_dydx(0, 1, t))
+    import os
+    old = os.environ.get("REDGB_CLUSTER")
+    os.environ["REDGB_CLUSTER"] = "0"
+    try:
+        with rg.Sim(s, dt=0.01, precision=precision, gas=gas) as sim:
+            return vec(sim.calc_dydx(0, 1, t))
+    finally:
+        if old is None:
+            del os.environ["REDGB_CLUSTER"]
+        else:
+            os.environ["REDGB_CLUSTER"] = old
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64_exact"])
