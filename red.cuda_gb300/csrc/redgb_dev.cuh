@@ -162,6 +162,7 @@ struct StageParams {
     int* head;            // stage 0 sets the collision check's bucket heads to -1 (not null)
     long long head_n;
     int cluster;          // 1: launched in clusters of kClusterChunks CTAs (items laid out for it)
+    int one_wave;         // 1: the launch is one wave (one kernel instance for every variant)
 };
 
 struct FinishParams {

@@ -828,6 +828,7 @@ StageParams red_sim::stage_params(int s, bool standalone)
     P.partial = partial;
     P.tile_cnt = tile_cnt;
     P.cluster = use_cluster ? 1 : 0;
+    P.one_wave = items.size() <= (size_t)6 * 152 ? 1 : 0;
     P.gas.enabled = cfg.gas_disk == 1;
     for (int k = 0; k < 2; k++) {
         P.gas.rho[k] = cfg.gas.rho[k];

@@ -147,24 +147,32 @@ __device__ __forceinline__ float2 ld_cluster_f2(const float2* local, unsigned ra
     return v;
 }
 
-// Operand slots of variant V: the stage velocity, y_r, y_v, then nk K_r and nk K_v.
-struct Ops {
-    int nk, KV;
-    __device__ explicit Ops(int V) : nk(var_nk(V)), KV(3 + var_nk(V)) {}
-    static constexpr int VS = 0, YR = 1, YV = 2, KR = 3;
-};
+// Operand slots of a variant: the stage velocity, y_r, y_v, then nk K_r and nk K_v.
+constexpr int kOpVS = 0, kOpYR = 1, kOpYV = 2, kOpKR = 3;
 // Source stages of the RKF7(8) combinations (Tableau::src), for runtime indexing.
 static __constant__ int c_src[13][kNkMax] = {
     {0}, {0}, {0, 1}, {0, 2}, {0, 2, 3}, {0, 3, 4}, {0, 3, 4, 5}, {0, 4, 5, 6},
     {0, 3, 4, 5, 6, 7}, {0, 3, 4, 5, 6, 7, 8}, {0, 3, 4, 5, 6, 7, 8, 9},
     {0, 5, 6, 7, 8, 9}, {0, 3, 4, 5, 6, 7, 8, 9, 11}};
-// Stage index of operand q of variant V.
+// Stage index of operand q of variant V: from the compile-time table when the
+// kernel instance fixes the variant (VT >= 0), else from constant memory.
+template <int VT>
 __device__ __forceinline__ int op_src(int V, int q)
 {
-    if (V >= 1 && V <= 12) return c_src[V][q];
-    if (V == 14) return q;
-    if (V == 15) return q == 0 ? 0 : (q == 1 ? 10 : 11);
-    return 3;
+    if constexpr (VT >= 1 && VT <= 12) {
+        return kSrc[VT][q];
+    } else if constexpr (VT == 14) {
+        return q;
+    } else if constexpr (VT == 15) {
+        return q == 0 ? 0 : (q == 1 ? 10 : 11);
+    } else if constexpr (VT >= 0) {
+        return 3;
+    } else {
+        if (V >= 1 && V <= 12) return c_src[V][q];
+        if (V == 14) return q;
+        if (V == 15) return q == 0 ? 0 : (q == 1 ? 10 : 11);
+        return 3;
+    }
 }
 
 // Gravity of the chunk's sources on SPT sinks per thread, FP32 modes.  The
@@ -368,13 +376,20 @@ __device__ __forceinline__ void gravity_f64(SmemStage& sm, const StageParams& P,
 // without holding registers.
 // ---------------------------------------------------------------------------
 // CL: the cluster-launch instance (FP32 modes), whose items are laid out in
-// clusters of kClusterChunks CTAs.
-template <int MODE, bool EXACT, bool CL>
-__global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const int V)
+// clusters of kClusterChunks CTAs.  VT >= 0 fixes the variant at compile time
+// (one instance per variant, for launches of many waves); VT = -1 takes it from
+// the launch argument, so that one kernel body serves all stages of a try and
+// stays in the instruction caches (launches of one wave, where the cold start
+// of each stage is on the critical path).
+template <int MODE, bool EXACT, bool CL, int VT>
+__global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const int Vrt)
 {
     constexpr bool kF32 = (MODE == MODE_MIXED || MODE == MODE_FP32);
+    const int V = VT >= 0 ? VT : Vrt;
     const bool kRkf = (V >= 1 && V <= 12);
-    const Ops O(V);
+    const int nk = var_nk(V);
+    const int kOpKV = 3 + nk;
+    constexpr int kUnroll = VT >= 0 ? kNkMax : 1;   // operand loops: unrolled when nk is a constant
     __shared__ SmemStage sm;
     __shared__ double ops[kOpsMax][kMaxElem];
     const GravItem it = P.items[blockIdx.x];
@@ -420,13 +435,14 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
     const bool need_vs = drag_on || V != 0;
     if (elem) {   // copy group 0: the operands older than the previous stage
         if (V >= 1 && V <= 14) {
-            cp_async8(&ops[O.YR][t], P.y_r + x);
-            cp_async8(&ops[O.YV][t], P.y_v + x);
+            cp_async8(&ops[kOpYR][t], P.y_r + x);
+            cp_async8(&ops[kOpYV][t], P.y_v + x);
         }
-        for (int q = 0; q < O.nk; q++) {
-            const int src = op_src(V, q);
-            if (src != s) cp_async8(&ops[O.KR + q][t], P.Kr[src] + x);
-            if (!(kRkf && src == V - 1) && src != s - 1) cp_async8(&ops[O.KV + q][t], P.Kv[src] + x);
+#pragma unroll kUnroll
+        for (int q = 0; q < nk; q++) {
+            const int src = op_src<VT>(V, q);
+            if (src != s) cp_async8(&ops[kOpKR + q][t], P.Kr[src] + x);
+            if (!(kRkf && src == V - 1) && src != s - 1) cp_async8(&ops[kOpKV + q][t], P.Kv[src] + x);
         }
     }
     cp_async_commit();
@@ -487,11 +503,12 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
     }
     cp_async_commit();
     if (elem) {   // copy group B: the operands the previous stage wrote
-        if (need_vs) cp_async8(&ops[O.VS][t], P.Kr[s] + x);
-        for (int q = 0; q < O.nk; q++) {
-            const int src = op_src(V, q);
-            if (src == s) cp_async8(&ops[O.KR + q][t], P.Kr[src] + x);
-            if (!(kRkf && src == V - 1) && src == s - 1) cp_async8(&ops[O.KV + q][t], P.Kv[src] + x);
+        if (need_vs) cp_async8(&ops[kOpVS][t], P.Kr[s] + x);
+#pragma unroll kUnroll
+        for (int q = 0; q < nk; q++) {
+            const int src = op_src<VT>(V, q);
+            if (src == s) cp_async8(&ops[kOpKR + q][t], P.Kr[src] + x);
+            if (!(kRkf && src == V - 1) && src == s - 1) cp_async8(&ops[kOpKV + q][t], P.Kv[src] + x);
         }
     }
     cp_async_commit();
@@ -654,7 +671,7 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
     if (!elem) return;
 
     // ---- element-wise FP64 epilogue ----
-    const double vs = need_vs ? ops[O.VS][t] : 0.0;   // stage velocity of the element
+    const double vs = need_vs ? ops[kOpVS][t] : 0.0;   // stage velocity of the element
     if (!(idi > 0)) a = 0.0;   // calc_grav_accel_naive zeroes inactive sinks (pp_disk.cu:386-388)
     if (drag_act) {
         const double g = ce == 0 ? sm.sc[ke][1] : (ce == 1 ? sm.sc[ke][2] : 0.0);
@@ -663,21 +680,22 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
     P.Kv[s][x] = a;
 
     if (V >= 1 && V <= 14) {
-        const double yr = ops[O.YR][t], yv = ops[O.YV][t];
+        const double yr = ops[kOpYR][t], yv = ops[kOpYV][t];
         double orr, ovv;
         if (kRkf) {
             // ytemp of stage V: y + dt * sum_q a_{V,q} K_q, terms in red's order
             // (rk8_kernel::calc_ytemp_for_f1..f12, int_rungekutta8.cu:80-246)
             const int off = 1 + V * (V - 1) / 2;
-            const int s0 = c_src[V][0];
-            const double kv0 = (s0 == V - 1) ? a : ops[O.KV][t];
-            double ar = mul<EXACT>(c_tb.a[off + s0], ops[O.KR][t]);
+            const int s0 = op_src<VT>(V, 0);
+            const double kv0 = (s0 == V - 1) ? a : ops[kOpKV][t];
+            double ar = mul<EXACT>(c_tb.a[off + s0], ops[kOpKR][t]);
             double av = mul<EXACT>(c_tb.a[off + s0], kv0);
-            for (int q = 1; q < O.nk; q++) {
-                const int sq = c_src[V][q];
+#pragma unroll kUnroll
+            for (int q = 1; q < nk; q++) {
+                const int sq = op_src<VT>(V, q);
                 const double aq = c_tb.a[off + sq];
-                const double kvq = (sq == V - 1) ? a : ops[O.KV + q][t];
-                ar = madd<EXACT>(ar, aq, ops[O.KR + q][t]);
+                const double kvq = (sq == V - 1) ? a : ops[kOpKV + q][t];
+                ar = madd<EXACT>(ar, aq, ops[kOpKR + q][t]);
                 av = madd<EXACT>(av, aq, kvq);
             }
             orr = madd<EXACT>(yr, dt, ar);
@@ -690,8 +708,8 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
         } else {
             // RK4 y_{n+1} as the positions of the adaptive stage 4
             const double b0 = mul<EXACT>(c_tb.b4[0], dt), b1 = mul<EXACT>(c_tb.b4[1], dt);
-            orr = rk4_ynp1<EXACT>(yr, b0, b1, ops[O.KR][t], ops[O.KR + 1][t], ops[O.KR + 2][t], vs);
-            ovv = rk4_ynp1<EXACT>(yv, b0, b1, ops[O.KV][t], ops[O.KV + 1][t], ops[O.KV + 2][t], a);
+            orr = rk4_ynp1<EXACT>(yr, b0, b1, ops[kOpKR][t], ops[kOpKR + 1][t], ops[kOpKR + 2][t], vs);
+            ovv = rk4_ynp1<EXACT>(yv, b0, b1, ops[kOpKV][t], ops[kOpKV + 1][t], ops[kOpKV + 2][t], a);
         }
         P.r_out[x] = orr;
         P.Kr[P.next][x] = ovv;
@@ -702,12 +720,12 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
             double er, ev;
             if (V == 15) {
                 // rk8_kernel::calc_error, int_rungekutta8.cu:248-260
-                er = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(ops[O.KR][t], ops[O.KR + 1][t]), ops[O.KR + 2][t]), vs));
-                ev = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(ops[O.KV][t], ops[O.KV + 1][t]), ops[O.KV + 2][t]), a));
+                er = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(ops[kOpKR][t], ops[kOpKR + 1][t]), ops[kOpKR + 2][t]), vs));
+                ev = fabs(sub<EXACT>(sub<EXACT>(add<EXACT>(ops[kOpKV][t], ops[kOpKV + 1][t]), ops[kOpKV + 2][t]), a));
             } else {
                 // rk4_kernel::calc_error, int_rungekutta4.cu:62-73
-                er = fabs(ops[O.KR][t] - vs);
-                ev = fabs(ops[O.KV][t] - a);
+                er = fabs(ops[kOpKR][t] - vs);
+                ev = fabs(ops[kOpKV][t] - a);
             }
             e = fmax(er, ev);
             if (er != er || ev != ev) e = __longlong_as_double(0x7ff8000000000000ll);
@@ -734,23 +752,54 @@ template <int MODE, bool EXACT>
 void stage_attributes()
 {
     static const bool done = [] {
-        cudaFuncSetAttribute(k_stage<MODE, EXACT, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(k_stage<MODE, EXACT, true, -1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         return true;
     }();
     (void)done;
 }
 
+template <int MODE, bool EXACT, int VT>
+void launch_fixed(const StageParams& P, int n, int v, cudaStream_t s)
+{
+    launch_k(k_stage<MODE, EXACT, false, VT>, (unsigned)n, (unsigned)kTile, s, P, v);
+}
+
+// A cluster plan takes the cluster instance, a plan of one wave the instance
+// with the variant as an argument, a plan of many waves the variant's own.
 template <int MODE, bool EXACT>
 void launch_stage_variant(const StageParams& P, int n, int v, cudaStream_t s)
 {
     if constexpr (MODE == MODE_MIXED || MODE == MODE_FP32) {
         if (P.cluster) {
             stage_attributes<MODE, EXACT>();
-            launch_kx(k_stage<MODE, EXACT, true>, (unsigned)n, (unsigned)kTile, (unsigned)kClusterChunks, s, P, v);
+            launch_kx(k_stage<MODE, EXACT, true, -1>, (unsigned)n, (unsigned)kTile, (unsigned)kClusterChunks, s, P,
+                      v);
             return;
         }
     }
-    launch_k(k_stage<MODE, EXACT, false>, (unsigned)n, (unsigned)kTile, s, P, v);
+    if (P.one_wave) {
+        launch_k(k_stage<MODE, EXACT, false, -1>, (unsigned)n, (unsigned)kTile, s, P, v);
+        return;
+    }
+    switch (v) {
+    case 1: launch_fixed<MODE, EXACT, 1>(P, n, v, s); break;
+    case 2: launch_fixed<MODE, EXACT, 2>(P, n, v, s); break;
+    case 3: launch_fixed<MODE, EXACT, 3>(P, n, v, s); break;
+    case 4: launch_fixed<MODE, EXACT, 4>(P, n, v, s); break;
+    case 5: launch_fixed<MODE, EXACT, 5>(P, n, v, s); break;
+    case 6: launch_fixed<MODE, EXACT, 6>(P, n, v, s); break;
+    case 7: launch_fixed<MODE, EXACT, 7>(P, n, v, s); break;
+    case 8: launch_fixed<MODE, EXACT, 8>(P, n, v, s); break;
+    case 9: launch_fixed<MODE, EXACT, 9>(P, n, v, s); break;
+    case 10: launch_fixed<MODE, EXACT, 10>(P, n, v, s); break;
+    case 11: launch_fixed<MODE, EXACT, 11>(P, n, v, s); break;
+    case 12: launch_fixed<MODE, EXACT, 12>(P, n, v, s); break;
+    case 13: launch_fixed<MODE, EXACT, 13>(P, n, v, s); break;
+    case 14: launch_fixed<MODE, EXACT, 14>(P, n, v, s); break;
+    case 15: launch_fixed<MODE, EXACT, 15>(P, n, v, s); break;
+    case 16: launch_fixed<MODE, EXACT, 16>(P, n, v, s); break;
+    default: launch_fixed<MODE, EXACT, 0>(P, n, v, s); break;
+    }
 }
 
 // Clusters of kClusterChunks stage CTAs that can be resident at once (FP32
@@ -771,7 +820,7 @@ int stage_active_clusters()
     cfg.attrs = at;
     cfg.numAttrs = 1;
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, k_stage<MODE, EXACT, true>, &cfg) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveClusters(&n, k_stage<MODE, EXACT, true, -1>, &cfg) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
