@@ -204,10 +204,17 @@ def roofline_for(rg, sim, systems, kw, peaks, traffic_per_launch):
     else:
         per_launch = 48 * n_body
     achieved = per_launch / (avg_ms * 1e-3) / 1e9
-    return {"kernel": names[dom], "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm, "traffic": traffic_per_launch.get(names[dom]), "avg_launch_ms": avg_ms,
-            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback",
-            "share": share}
+    out = {"kernel": names[dom], "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+           "frac": achieved / hbm, "traffic": traffic_per_launch.get(names[dom]), "avg_launch_ms": avg_ms,
+           "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback",
+           "share": share}
+    if names[dom] == "stage":
+        # the same launch against the FP32 pipe: 20 FLOP per directed interaction
+        tflops = 20.0 * sim.interactions_per_eval / (avg_ms * 1e-3) / 1e12
+        peak32 = FP32_NOMINAL_TFLOPS
+        out["gravity_fp32"] = {"achieved": tflops, "peak": peak32, "unit": "TFLOP/s", "frac": tflops / peak32,
+                               "peak_source": "nominal: 152 SMs x 128 FP32 lanes x 2 FLOP x 2.07 GHz"}
+    return out
 
 
 def cpu_baseline_sample(systems, kw, seconds=10.0):
@@ -245,6 +252,7 @@ def cpu_baseline_sample(systems, kw, seconds=10.0):
             "sim_years_per_s": sim_t / K_GAUSS / YEAR / el}
 
 
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12   # GB300 FP32 FMA, nominal
 PROPOSER_WARMUP_TRIES = 400   # tries before the timed region in the learned-proposal workload
 
 
