@@ -81,8 +81,10 @@ enum {
 };
 
 typedef struct {
-    int32_t integrator;          /* RED_INTEGRATOR_RUNGEKUTTA4 or _RUNGEKUTTAFEHLBERG78 (options.cpp:297-326) */
-    int32_t adaptive;            /* integrator ctor argument (int_rungekutta4.cu:101, int_rungekutta8.cu:405) */
+    int32_t integrator;          /* RED_INTEGRATOR_EULER, _RUNGEKUTTA2, _RUNGEKUTTA4 or _RUNGEKUTTAFEHLBERG78
+                                    (options.cpp:297-326) */
+    int32_t adaptive;            /* integrator ctor argument (int_rungekutta4.cu:101, int_rungekutta8.cu:405);
+                                    Euler and RK2 are fixed-step, as red's constructors make them */
     double tolerance;
     int32_t error_check_for_tp;  /* integrator::error_check_for_tp (integrator.h:33) */
     int32_t precision;           /* RED_PREC_* */

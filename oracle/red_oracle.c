@@ -414,6 +414,69 @@ static int step_rk4(orc_integrator* ig, double* t, const uint32_t pl[7], const o
     return ORC_OK;
 }
 
+/* euler::step, int_euler.cu:73-105: f0 = f(t, y); y_{n+1} = y + dt_try f0
+   (euler::cpu_sum_vector, :34-40); the step size stays the constructor's
+   dt_try, and dt_next = dt_try after the step */
+static int step_euler(orc_integrator* ig, double* t, const uint32_t pl[7], const orc_bmd* md,
+                      const orc_param* p, const orc_gas* gas, orc_var4* r, orc_var4* v, orc_work* w)
+{
+    const uint32_t n_body = orc_n_total(pl);
+    const uint32_t n_var = 4 * n_body;
+    int rc = dydx_both(ig, *t, pl, md, p, gas, r, v, w->fr[0], w->fv[0]);
+    if (rc) return rc;
+    const double bf = ig->dt_try;
+    for (int half = 0; half < 2; half++) {
+        const double* y = (const double*)(half ? v : r);
+        const double* f = (const double*)(half ? w->fv[0] : w->fr[0]);
+        double* o = (double*)(half ? w->outv : w->outr);
+        for (uint32_t k = 0; k < n_var; k++) o[k] = y[k] + bf * f[k];
+    }
+    ig->dt_did = ig->dt_try;
+    ig->dt_next = ig->dt_try;
+    ig->n_tried += 1; ig->n_passed++;   /* update_counters(1), integrator.cu:270-275 */
+    *t += ig->dt_did;
+    memcpy(r, w->outr, n_body * sizeof(orc_var4));
+    memcpy(v, w->outv, n_body * sizeof(orc_var4));
+    return ORC_OK;
+}
+
+/* rungekutta2::step, int_rungekutta2.cu:91-131, with a = {0, 1/2}, b = {0, 1},
+   c = {0, 1/2} (:12-14): f1 = f(t, y); ytemp = y + (a1 dt) f1
+   (calc_ytemp_for_fr, :47-64); f2 = f(t + c1 dt, ytemp); y_{n+1} = y + (b1 dt) f2
+   (calc_y_np1, :66-83); fixed step as in euler::step */
+static const double rk2_a[2] = {0.0, 1.0 / 2.0}, rk2_b[2] = {0.0, 1.0}, rk2_c[2] = {0.0, 1.0 / 2.0};
+static int step_rk2(orc_integrator* ig, double* t, const uint32_t pl[7], const orc_bmd* md,
+                    const orc_param* p, const orc_gas* gas, orc_var4* r, orc_var4* v, orc_work* w)
+{
+    const uint32_t n_body = orc_n_total(pl);
+    const uint32_t n_var = 4 * n_body;
+    int rc = dydx_both(ig, *t + rk2_c[0] * ig->dt_try, pl, md, p, gas, r, v, w->fr[0], w->fv[0]);
+    if (rc) return rc;
+    const double af = rk2_a[1] * ig->dt_try;
+    for (int half = 0; half < 2; half++) {
+        const double* y = (const double*)(half ? v : r);
+        const double* f = (const double*)(half ? w->fv[0] : w->fr[0]);
+        double* o = (double*)(half ? w->yv_t : w->yr_t);
+        for (uint32_t k = 0; k < n_var; k++) o[k] = y[k] + af * f[k];
+    }
+    rc = dydx_both(ig, *t + rk2_c[1] * ig->dt_try, pl, md, p, gas, w->yr_t, w->yv_t, w->fr[1], w->fv[1]);
+    if (rc) return rc;
+    const double bf = rk2_b[1] * ig->dt_try;
+    for (int half = 0; half < 2; half++) {
+        const double* y = (const double*)(half ? v : r);
+        const double* f = (const double*)(half ? w->fv[1] : w->fr[1]);
+        double* o = (double*)(half ? w->outv : w->outr);
+        for (uint32_t k = 0; k < n_var; k++) o[k] = y[k] + bf * f[k];
+    }
+    ig->dt_did = ig->dt_try;
+    ig->dt_next = ig->dt_try;
+    ig->n_tried += 1; ig->n_passed++;
+    *t += ig->dt_did;
+    memcpy(r, w->outr, n_body * sizeof(orc_var4));
+    memcpy(v, w->outv, n_body * sizeof(orc_var4));
+    return ORC_OK;
+}
+
 /* ytemp = y_n + dt*(sum_s a_rs f_s) in red's term order */
 static void rk8_stage_combine(int rs, double dt, uint32_t n_var, const double* y, double* const* f, double* out)
 {
@@ -498,6 +561,12 @@ int orc_step(orc_integrator* ig, double* t, const uint32_t pl[7], const orc_bmd*
     } else if (ig->type == ORC_RKF78) {
         if ((rc = work_alloc(&w, n, ig->adaptive ? 13 : 11))) { work_free(&w); return rc; }
         rc = step_rk8(ig, t, pl, md, p, gas, r, v, &w);
+    } else if (ig->type == ORC_EULER) {
+        if ((rc = work_alloc(&w, n, 1))) { work_free(&w); return rc; }
+        rc = step_euler(ig, t, pl, md, p, gas, r, v, &w);
+    } else if (ig->type == ORC_RK2) {
+        if ((rc = work_alloc(&w, n, 2))) { work_free(&w); return rc; }
+        rc = step_rk2(ig, t, pl, md, p, gas, r, v, &w);
     } else {
         return ORC_ERR_NOT_IMPLEMENTED;
     }

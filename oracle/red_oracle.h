@@ -94,7 +94,7 @@ int orc_calc_dydx(int sem, int i, double t, const uint32_t playing[7], const orc
 
 /* --- integrators ------------------------------------------------------------ */
 typedef struct {
-    int32_t type;              /* ORC_RK4 or ORC_RKF78 */
+    int32_t type;              /* ORC_EULER, ORC_RK2 (fixed step), ORC_RK4 or ORC_RKF78 */
     int32_t adaptive;
     int32_t error_check_for_tp;
     int32_t sem;               /* ORC_SEM_GPU or ORC_SEM_CPU */

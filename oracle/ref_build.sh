@@ -25,6 +25,8 @@ INC="-I$REF/red.type -I$REF/src/red.cuda.utility -I$REF/src/red.cuda"
 SRCS="
 $REF/src/red.cuda/pp_disk.cu
 $REF/src/red.cuda/integrator.cu
+$REF/src/red.cuda/int_euler.cu
+$REF/src/red.cuda/int_rungekutta2.cu
 $REF/src/red.cuda/int_rungekutta4.cu
 $REF/src/red.cuda/int_rungekutta8.cu
 $REF/src/red.cuda/analytic_gas_disk.cu

@@ -13,7 +13,7 @@
 //   dir=  info=  data=            red input files (ASCII .txt or binary .dat)
 //   out=                          output file (raw little-endian records)
 //   mode=accel|run|coll|ejhc|integral|dump
-//   integrator=4|8 adaptive=0|1 tol= nsteps= eftp=0|1   (mode=run)
+//   integrator=1|2|4|8 (Euler, RK2, RK4, RKF78) adaptive=0|1 tol= nsteps= eftp=0|1   (mode=run)
 //   factor= t=                    (mode=coll)
 //   ej= hc=                       (mode=ejhc)
 //   gasdir= gas= t=               (mode=accel: adds drag on NSI bodies)
@@ -29,6 +29,8 @@
 #define private public
 #include "pp_disk.h"
 #include "integrator.h"
+#include "int_euler.h"
+#include "int_rungekutta2.h"
 #include "int_rungekutta4.h"
 #include "int_rungekutta8.h"
 #undef private
@@ -121,7 +123,9 @@ int main(int argc, char** argv)
             var_t tol = atof(arg("tol", "1e-10").c_str());
             int nsteps = atoi(arg("nsteps", "1").c_str());
             integrator* ig = 0;
-            if (kind == 4) ig = new rungekutta4(ppd, ppd->dt, adaptive, tol, COMPUTING_DEVICE_CPU);
+            if (kind == 1) ig = new euler(ppd, ppd->dt, COMPUTING_DEVICE_CPU);
+            else if (kind == 2) ig = new rungekutta2(ppd, ppd->dt, COMPUTING_DEVICE_CPU);
+            else if (kind == 4) ig = new rungekutta4(ppd, ppd->dt, adaptive, tol, COMPUTING_DEVICE_CPU);
             else ig = new rungekutta8(ppd, ppd->dt, adaptive, tol, COMPUTING_DEVICE_CPU);
             ig->error_check_for_tp = atoi(arg("eftp", "0").c_str()) != 0;
             put(f, &nsteps, 4);

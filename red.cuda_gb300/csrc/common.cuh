@@ -282,65 +282,12 @@ struct alignas(32) D4 {
 
 // Nonzero terms of each RKF7(8) stage row in the order red's stage kernels
 // add them (rk8_kernel::calc_ytemp_for_f1..f12, int_rungekutta8.cu:80-246).
-// Compile-time copies of Tableau::nnz / src so that the combination unrolls.
-__device__ constexpr int kNnz[13] = {0, 1, 2, 2, 3, 3, 4, 4, 6, 7, 8, 6, 9};
+// Compile-time copy of Tableau::src (the source stages of each RKF7(8)
+// combination, in red's term order), for the per-variant kernel instances.
 __device__ constexpr int kSrc[13][9] = {
     {0}, {0}, {0, 1}, {0, 2}, {0, 2, 3}, {0, 3, 4}, {0, 3, 4, 5}, {0, 4, 5, 6},
     {0, 3, 4, 5, 6, 7}, {0, 3, 4, 5, 6, 7, 8}, {0, 3, 4, 5, 6, 7, 8, 9},
     {0, 5, 6, 7, 8, 9}, {0, 3, 4, 5, 6, 7, 8, 9, 11}};
-
-// Component x (= 3 i + c) of the ytemp of RKF7(8) stage NX:
-// y + dt * sum_q a_{NX,q} K_q, terms in red's order; loads issued first.
-template <int NX, bool EXACT>
-__device__ __forceinline__ void combine_rkf78(const StageParams& P, double dt, int x, double& out_r, double& out_v)
-{
-    constexpr int nnz = kNnz[NX];
-    constexpr int off = 1 + NX * (NX - 1) / 2;
-    double kr[nnz], kv[nnz];
-#pragma unroll
-    for (int q = 0; q < nnz; q++) {
-        kr[q] = P.Kr[kSrc[NX][q]][x];
-        kv[q] = P.Kv[kSrc[NX][q]][x];
-    }
-    double ar = mul<EXACT>(c_tb.a[off + kSrc[NX][0]], kr[0]);
-    double av = mul<EXACT>(c_tb.a[off + kSrc[NX][0]], kv[0]);
-#pragma unroll
-    for (int q = 1; q < nnz; q++) {
-        const double aq = c_tb.a[off + kSrc[NX][q]];
-        ar = madd<EXACT>(ar, aq, kr[q]);
-        av = madd<EXACT>(av, aq, kv[q]);
-    }
-    out_r = madd<EXACT>(P.y_r[x], dt, ar);
-    out_v = madd<EXACT>(P.y_v[x], dt, av);
-}
-
-// Component x of the ytemp of stage nx (RKF78: y + dt*sum a K in red's term
-// order; RK4: y + (a dt) K, rk4_kernel::sum_vector, int_rungekutta4.cu:36-47).
-template <bool EXACT>
-__device__ __forceinline__ void combine(const StageParams& P, int scheme, int nx, double dt, int x, double& out_r,
-                                        double& out_v)
-{
-    if (scheme == SCHEME_RKF78) {
-        switch (nx) {
-        case 1: combine_rkf78<1, EXACT>(P, dt, x, out_r, out_v); break;
-        case 2: combine_rkf78<2, EXACT>(P, dt, x, out_r, out_v); break;
-        case 3: combine_rkf78<3, EXACT>(P, dt, x, out_r, out_v); break;
-        case 4: combine_rkf78<4, EXACT>(P, dt, x, out_r, out_v); break;
-        case 5: combine_rkf78<5, EXACT>(P, dt, x, out_r, out_v); break;
-        case 6: combine_rkf78<6, EXACT>(P, dt, x, out_r, out_v); break;
-        case 7: combine_rkf78<7, EXACT>(P, dt, x, out_r, out_v); break;
-        case 8: combine_rkf78<8, EXACT>(P, dt, x, out_r, out_v); break;
-        case 9: combine_rkf78<9, EXACT>(P, dt, x, out_r, out_v); break;
-        case 10: combine_rkf78<10, EXACT>(P, dt, x, out_r, out_v); break;
-        case 11: combine_rkf78<11, EXACT>(P, dt, x, out_r, out_v); break;
-        default: combine_rkf78<12, EXACT>(P, dt, x, out_r, out_v); break;
-        }
-    } else {
-        const double bf = mul<EXACT>(c_tb.a4[nx], dt);
-        out_r = madd<EXACT>(P.y_r[x], bf, P.Kr[nx - 1][x]);
-        out_v = madd<EXACT>(P.y_v[x], bf, P.Kv[nx - 1][x]);
-    }
-}
 
 // RK4 y_{n+1} = y + b0 (f1 + f4) + b1 (f2 + f3), b = (1/6, 1/3) * dt
 // (rk4_kernel::calc_y_np1, int_rungekutta4.cu:49-60)

@@ -90,7 +90,8 @@ __global__ void k_control(const ControlParams P)
     if (S.quota > 0) S.quota--;
     if (P.output_interval != 0.0 && fabs(P.output_interval) < fabs(S.dt_next))
         S.dt_next = 0.0 < dt ? P.output_interval : -P.output_interval;
-    S.dt_try = S.dt_next;
+    // euler::step / rungekutta2::step take dt_try, never dt_next (int_euler.cu:73-105)
+    if (!P.keep_dt) S.dt_try = S.dt_next;
     if (P.length != 0.0 && fabs(S.t - S.t_start) > fabs(P.length)) S.active = 0;
 }
 
@@ -150,6 +151,15 @@ __global__ void __launch_bounds__(4 * kFinishBodies) k_finish(const FinishParams
         if (P.scheme == SCHEME_RKF78) {
             r = rk8_ynp1<EXACT>(P.y_r[x], dt, P.Kr, x);
             v = rk8_ynp1<EXACT>(P.y_v[x], dt, P.Kv, x);
+        } else if (P.scheme == SCHEME_EULER) {
+            // euler::calc_y_np1 -> sum_vector, int_euler.cu:19-31, 54-71: y + dt f0
+            r = madd<EXACT>(P.y_r[x], dt, P.Kr[0][x]);
+            v = madd<EXACT>(P.y_v[x], dt, P.Kv[0][x]);
+        } else if (P.scheme == SCHEME_RK2) {
+            // rungekutta2::calc_y_np1, int_rungekutta2.cu:66-83: y + (b_1 dt) f2
+            const double bf = mul<EXACT>(c_tb.b2[1], dt);
+            r = madd<EXACT>(P.y_r[x], bf, P.Kr[1][x]);
+            v = madd<EXACT>(P.y_v[x], bf, P.Kv[1][x]);
         } else if (P.commit_from_stage4) {
             r = P.t_r0[x];
             v = P.Kr[4][x];

@@ -24,7 +24,7 @@ constexpr int kClusterChunks = 16;  // source chunks of a tile in a cluster laun
 constexpr int kMaxStages = 13;
 
 enum Mode { MODE_MIXED = 0, MODE_FP64 = 1, MODE_FP64_EXACT = 2, MODE_FP32 = 3 };
-enum Scheme { SCHEME_RK4 = 0, SCHEME_RKF78 = 1 };
+enum Scheme { SCHEME_RK4 = 0, SCHEME_RKF78 = 1, SCHEME_EULER = 2, SCHEME_RK2 = 3 };
 enum Cls { CLS_SI = 0, CLS_NSI = 1, CLS_NI = 2 };
 
 // Per-system integrator state, device resident.  Mirrors integrator's
@@ -127,6 +127,8 @@ struct Tableau {
     int src[kMaxStages][9];
     // RK4, int_rungekutta4.cu:26-31
     double a4[8], b4[5], c4[5];
+    // RK2, int_rungekutta2.cu:12-14 (Euler has no coefficients: y + dt f)
+    double a2[2], b2[2], c2[2];
 };
 
 struct StageParams {
@@ -193,6 +195,7 @@ struct FinishParams {
 struct ControlParams {
     int n_sys;
     int scheme, adaptive, order;
+    int keep_dt;          // Euler / RK2: every step takes the initial dt (the dt_next clamp does not feed back)
     double tolerance, lambda;
     double output_interval, length;
     DevSys* sys;

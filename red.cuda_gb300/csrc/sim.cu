@@ -103,6 +103,11 @@ Tableau make_tableau()
     memcpy(t.a4, a4, sizeof(a4));
     memcpy(t.b4, b4, sizeof(b4));
     memcpy(t.c4, c4, sizeof(c4));
+    // int_rungekutta2.cu:12-14
+    const double a2[2] = {0.0, 1.0 / 2.0}, b2[2] = {0.0, 1.0}, c2[2] = {0.0, 1.0 / 2.0};
+    memcpy(t.a2, a2, sizeof(a2));
+    memcpy(t.b2, b2, sizeof(b2));
+    memcpy(t.c2, c2, sizeof(c2));
     return t;
 }
 
@@ -527,8 +532,18 @@ void red_sim::create(const red_config_t* c, uint32_t n_systems, const uint32_t* 
         n_stage = cfg.adaptive ? 13 : 11;
         order = 7;
         lambda = 41.0 / 840.0;
+    } else if (cfg.integrator == RED_INTEGRATOR_EULER || cfg.integrator == RED_INTEGRATOR_RUNGEKUTTA2) {
+        // euler / rungekutta2 (int_euler.cu:42-47, int_rungekutta2.cu:39-44) are
+        // fixed-step only: their constructors pass adaptive = false
+        const bool eu = cfg.integrator == RED_INTEGRATOR_EULER;
+        scheme = eu ? SCHEME_EULER : SCHEME_RK2;
+        n_stage = eu ? 1 : 2;
+        order = eu ? 1 : 2;
+        lambda = 0.0;
+        cfg.adaptive = 0;
     } else {
-        throw ArgError{RED_ERR_NOT_IMPLEMENTED, "only RUNGEKUTTA4 and RUNGEKUTTAFEHLBERG78 are on this path"};
+        throw ArgError{RED_ERR_NOT_IMPLEMENTED, "integrator not on this path (EULER, RUNGEKUTTA2, RUNGEKUTTA4, "
+                                                "RUNGEKUTTAFEHLBERG78 are)"};
     }
     if (cfg.precision < 0 || cfg.precision > 3) throw ArgError{RED_ERR_ARG, "bad precision"};
     mode = cfg.precision;
@@ -883,6 +898,7 @@ void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs
     C.scheme = scheme;
     C.adaptive = cfg.adaptive;
     C.order = order;
+    C.keep_dt = (scheme == SCHEME_EULER || scheme == SCHEME_RK2) ? 1 : 0;
     C.tolerance = cfg.tolerance;
     C.lambda = lambda;
     C.output_interval = cfg.output_interval;

@@ -133,6 +133,15 @@ __host__ __device__ constexpr int var_nk(int v)
 }
 constexpr int kNkMax = 9;                  // the most K operands of a variant (RKF7(8) stage 12)
 constexpr int kOpsMax = 3 + 2 * kNkMax;    // shared-memory operand slots
+// The time offset c_s of stage s (RKF7(8), RK4, RK2; Euler evaluates at t).
+__device__ __forceinline__ double stage_c(int scheme, int s)
+{
+    if (scheme == SCHEME_RKF78) return c_tb.c[s];
+    if (scheme == SCHEME_RK4) return c_tb.c4[s];
+    if (scheme == SCHEME_RK2) return c_tb.c2[s];
+    return 0.0;
+}
+
 // Thread-block cluster helpers (a tile's source chunks as one cluster): the
 // barrier in two halves (every thread of every CTA of the cluster arrives;
 // release / acquire at cluster scope) and a read of another CTA's shared memory.
@@ -517,7 +526,7 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
     double decr = 0.0;
     if (drag_on) {
         const double ts = P.standalone ? P.t_standalone
-                                       : tsys + (P.scheme == SCHEME_RKF78 ? c_tb.c[s] : c_tb.c4[s]) * dt;
+                                       : tsys + stage_c(P.scheme, s) * dt;
         decr = gas_reduction_factor(P.gas, ts);
     }
     const bool drag_act = drag_on && !(1.0e-6 > decr);
@@ -702,7 +711,7 @@ __global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const i
             ovv = madd<EXACT>(yv, dt, av);
         } else if (V == 13) {
             // rk4_kernel::sum_vector, int_rungekutta4.cu:36-47: y + (a dt) K_s
-            const double bf = mul<EXACT>(c_tb.a4[s + 1], dt);
+            const double bf = mul<EXACT>(P.scheme == SCHEME_RK2 ? c_tb.a2[s + 1] : c_tb.a4[s + 1], dt);
             orr = madd<EXACT>(yr, bf, vs);
             ovv = madd<EXACT>(yv, bf, a);
         } else {

@@ -19,7 +19,7 @@ ERRORS = {1: "RED_ERR_ARG", 2: "RED_ERR_CUDA", 3: "RED_ERR_EVENT_OVERFLOW", 4: "
           5: "RED_ERR_NONFINITE", 6: "RED_ERR_NOT_IMPLEMENTED", 7: "RED_ERR_SUPERPLANETESIMAL",
           8: "RED_ERR_NO_DEVICE"}
 PRECISION = {"mixed": 0, "fp64": 1, "fp64_exact": 2, "fp32": 3}
-INTEGRATOR = {"rk4": 2, "rkf78": 4, "rkf8": 4}
+INTEGRATOR = {"euler": 0, "e": 0, "rk2": 1, "rk4": 2, "rkf78": 4, "rkf8": 4}
 
 EXPORTS = ["red_create", "red_destroy", "red_step", "red_launch_tries", "red_synchronize",
            "red_handle_events", "red_check_for_collision", "red_check_for_ejection_hit_centrum",

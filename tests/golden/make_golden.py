@@ -223,6 +223,8 @@ def main():
         case_run(tmp, "rkf78_adaptive", 8, 1, 1e-10, 5.0, 25)
         case_run(tmp, "rkf78_adaptive_tp", 8, 1, 1e-12, 5.0, 12, eftp=1)
         case_run(tmp, "rkf78_fixed", 8, 0, 0.0, 4.0, 20)
+        case_run(tmp, "euler_fixed", 1, 0, 0.0, 0.05, 40)
+        case_run(tmp, "rk2_fixed", 2, 0, 0.0, 0.2, 40)
         case_collision(tmp)
         case_ejhc(tmp)
         case_integral(tmp)

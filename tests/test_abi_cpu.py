@@ -66,6 +66,6 @@ def test_create_validates_inputs_before_touching_the_device(rg):
         else:
             raise AssertionError("expected an error")
     try:
-        rg.Sim(s, dt=0.1, integrator=0)     # Euler is not on this path
+        rg.Sim(s, dt=0.1, integrator=3)     # no integrator of red has this code
     except rg.RedError as e:
         assert e.code == 6

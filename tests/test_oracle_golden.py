@@ -61,11 +61,11 @@ def test_drag_bitexact(orc):
 
 
 @pytest.mark.parametrize("name", ["rk4_fixed", "rk4_adaptive", "rkf78_adaptive",
-                                  "rkf78_adaptive_tp", "rkf78_fixed"])
+                                  "rkf78_adaptive_tp", "rkf78_fixed", "euler_fixed", "rk2_fixed"])
 def test_integrator_bitexact(orc, name):
     g = golden(name + ".npz")
     b = body(orc, g)
-    kind = orc.RK4 if int(g["integrator"]) == 4 else orc.RKF78
+    kind = {1: orc.EULER, 2: orc.RK2, 4: orc.RK4, 8: orc.RKF78}[int(g["integrator"])]
     ig = orc.make_integrator(kind, float(g["dt0"]), adaptive=bool(g["adaptive"]), tol=float(g["tol"]),
                              error_check_for_tp=bool(g["eftp"]), sem=orc.SEM_CPU)
     t = 0.0
