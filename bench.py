@@ -320,7 +320,20 @@ def run_reference(args, rg, rank, world):
 def run_ours(args, rg, rank, world, local_rank):
     import torch
     torch.cuda.set_device(local_rank)
+    t_ic = time.perf_counter()
     systems, kw, desc = workload(rg, args.config, rank, world)
+    t_ic = time.perf_counter() - t_ic
+    ic_gpu = None
+    if args.config in ("c4", "c5"):
+        # the same ensemble layout drawn by the GPU generator (red_populate_disks)
+        first, count = rg.shard.ensemble_range(512, rank, world)
+        rg.ic.config4_gpu(n_systems=1, first=first, device=local_rank)   # first call: library and context warm
+        t_gpu = time.perf_counter()
+        gen = rg.ic.config4_gpu(n_systems=count, first=first, device=local_rank)
+        t_gpu = time.perf_counter() - t_gpu
+        ic_gpu = {"bodies": int(sum(s.n for s in gen)), "host_numpy_s": t_ic, "gpu_s": t_gpu,
+                  "api": "red_populate_disks (records copied to host memory)"}
+        del gen
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -438,6 +451,8 @@ def run_ours(args, rg, rank, world, local_rank):
                 "vs_plain_fp64": (value / fp64["value"]) if fp64 else None,
                 "clocks": clk,
                 "gpu_launches": int(launches)}
+        if ic_gpu is not None:
+            line["initial_conditions"] = ic_gpu
         if proposer is not None:
             plain = plain_comparison(rg, systems, kw, args, local_rank, stream, flush)
             line["proposer"] = {

@@ -205,6 +205,37 @@ uint32_t red_n_systems(red_sim* sim);
    bookkeeping: no device synchronisation.  0 for a bad handle or index. */
 uint32_t red_n_bodies(red_sim* sim, uint32_t sys);
 
+/* ---- initial conditions of disk ensembles -------------------------------
+ * red.cuda.initial's disk recipe (populate_disk, red.cuda.initial/main.cu:251-314;
+ * calculate_phase, main.cu:317-342; distribution.cpp:11-204) on the GPU, one
+ * thread per body: a star, n_pp protoplanets and n_pl planetesimals per
+ * system, sorted by type.  Orbital elements: protoplanet semi-major axes
+ * pp_a0 * f^k (f for pp_hill mutual Hill radii, pp_hill > 0) or pp_a0 + k pp_da;
+ * planetesimal a uniform (pl_a_log = 0) or log-uniform in [pl_a_min, pl_a_max];
+ * e and i Rayleigh (sigma_*), e capped at e_max; peri, node, mean anomaly
+ * uniform in [0, 2 pi).  Planetesimal masses m_j = pl_mass_total a_j^pl_mass_exp
+ * / sum_j a_j^pl_mass_exp.  Kepler -> Cartesian with mu = K^2 (m_star + m)
+ * (tools.cpp:789-828), the system moved to its barycentre (tools.cpp:413-434),
+ * velocities divided by K (red.cuda.initial/main.cu:1666-1670).  Random
+ * numbers: Philox4x32-10 (Salmon et al., SC'11), key = seed, counter = (body,
+ * draw), so every body's draws are independent of the launch shape.  Output:
+ * red's records for all systems, concatenated (1 + n_pp + n_pl each), and 7
+ * playing counts per system. */
+typedef struct {
+    uint32_t n_pp, n_pl;
+    double m_star, star_radius;                /* M_sun, AU */
+    double pp_mass, pp_a0, pp_da, pp_hill;
+    double pl_a_min, pl_a_max;
+    int32_t pl_a_log, pad;
+    double pl_mass_total, pl_mass_exp;
+    double sigma_e_pp, sigma_i_pp, sigma_e, sigma_i, e_max;
+    double density;                            /* g/cm^3, protoplanets and planetesimals */
+    double cd;                                 /* planetesimals */
+    uint64_t seed;
+} red_disk_spec_t;
+int red_populate_disks(const red_disk_spec_t* specs, uint32_t n_systems, int32_t device, uint32_t* playing,
+                       red_var4_t* r, red_var4_t* v, red_param_t* p, red_body_metadata_t* md);
+
 /* ---- allocation-free gravity ---------------------------------------------
  * No counterpart in red.  For callers that cannot call cudaMalloc (device
  * memory owned by another pool, real-time loops that must not enter the

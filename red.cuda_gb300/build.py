@@ -21,7 +21,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
               "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 UNITS = ["stage_mixed.cu", "stage_fp64.cu", "stage_exact.cu", "stage_fp32.cu", "kernels.cu", "sim.cu", "noalloc.cu",
-         "proposer.cu"]
+         "proposer.cu", "populate.cu"]
 # The FP32 gravity of the MIXED and FP32 modes flushes FP32 denormals (|x| < 1.2e-38, far below any
 # coordinate difference, mass or acceleration of the path), so rsqrtf is the bare hardware reciprocal
 # square root; FP64 arithmetic is not affected by the flag.

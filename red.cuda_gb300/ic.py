@@ -196,6 +196,32 @@ def config4(n_systems=512, n_min=128, n_max=4096, first=0):
     return [config4_system(first + i, n_min, n_max) for i in range(n_systems)]
 
 
+def config4_specs(n_systems=512, n_min=128, n_max=4096, first=0):
+    """red_populate_disks specifications of the config-4 ensemble: the same
+    system sizes as config4 (drawn from the same seeds), the bodies drawn on
+    the GPU from Philox streams keyed by 1000 + i (a different realisation of
+    the same recipe)."""
+    from .lib import DiskSpec
+    out = []
+    for i in range(first, first + n_systems):
+        rng = np.random.Generator(np.random.MT19937(1000 + i))
+        n = int(rng.integers(n_min, n_max + 1))
+        n_pp = int(rng.integers(2, 9))
+        n_pl = n - 1 - n_pp
+        out.append(DiskSpec(n_pp=n_pp, n_pl=n_pl, m_star=1.0, star_radius=SOLAR_RADIUS_TO_AU,
+                            pp_mass=0.1 * EARTH_TO_SOLAR, pp_a0=0.8, pp_da=0.2, pp_hill=0.0, pl_a_min=0.7,
+                            pl_a_max=1.5, pl_a_log=0, pl_mass_total=EARTH_TO_SOLAR, pl_mass_exp=0.0,
+                            sigma_e_pp=0.01, sigma_i_pp=0.005, sigma_e=0.01, sigma_i=0.005, e_max=0.9,
+                            density=2.0, cd=0.0, seed=1000 + i))
+    return out
+
+
+def config4_gpu(n_systems=512, n_min=128, n_max=4096, first=0, device=0):
+    """The config-4 ensemble generated on the GPU (red_populate_disks)."""
+    from .lib import populate_disks
+    return populate_disks(config4_specs(n_systems, n_min, n_max, first), device=device)
+
+
 def gas_disk_config3():
     """MMSN-like analytic gas disk of config 3 as red's analytic_gas_disk file
     keys (analytic_gas_disk.cu:99-246): Sigma_0 = 1700 g/cm^2, h/r = 0.05,

@@ -29,6 +29,7 @@ EXPORTS = ["red_create", "red_destroy", "red_step", "red_launch_tries", "red_syn
            "red_n_bodies",
            "red_calc_accel_noalloc", "red_mlp_param_count", "red_mlp_predict", "red_mlp_grad", "red_mlp_adam",
            "red_set_step_proposer", "red_clear_step_proposer", "red_log_features", "red_get_feature_log",
+           "red_populate_disks",
            "red_last_error", "red_version"]
 
 
@@ -72,6 +73,16 @@ class AccelArgs(C.Structure):
 
 
 NOALLOC_MAX_BODIES = 32768
+
+
+class DiskSpec(C.Structure):
+    """red_disk_spec_t: one disk of red_populate_disks."""
+    _fields_ = [("n_pp", C.c_uint32), ("n_pl", C.c_uint32), ("m_star", C.c_double), ("star_radius", C.c_double),
+                ("pp_mass", C.c_double), ("pp_a0", C.c_double), ("pp_da", C.c_double), ("pp_hill", C.c_double),
+                ("pl_a_min", C.c_double), ("pl_a_max", C.c_double), ("pl_a_log", C.c_int32), ("pad", C.c_int32),
+                ("pl_mass_total", C.c_double), ("pl_mass_exp", C.c_double), ("sigma_e_pp", C.c_double),
+                ("sigma_i_pp", C.c_double), ("sigma_e", C.c_double), ("sigma_i", C.c_double), ("e_max", C.c_double),
+                ("density", C.c_double), ("cd", C.c_double), ("seed", C.c_uint64)]
 
 
 class MlpNorm(C.Structure):
@@ -126,6 +137,7 @@ def load(path=LIB_PATH):
     L.red_n_bodies.argtypes = [P, C.c_uint32]
     L.red_n_bodies.restype = C.c_uint32
     L.red_calc_accel_noalloc.argtypes = [C.POINTER(AccelArgs)]
+    L.red_populate_disks.argtypes = [C.POINTER(DiskSpec), C.c_uint32, C.c_int32, P, P, P, P, P]
     L.red_mlp_param_count.restype = C.c_uint32
     L.red_mlp_predict.argtypes = [P, C.POINTER(MlpNorm), P, P, C.c_uint32, P]
     L.red_mlp_grad.argtypes = [P, P, P, C.c_uint32, P, P, P]
@@ -152,6 +164,25 @@ def _check(rc):
 def calc_accel_noalloc(args):
     """Calls red_calc_accel_noalloc with a filled AccelArgs; raises on error."""
     _check(load().red_calc_accel_noalloc(C.byref(args)))
+
+
+def populate_disks(specs, device=0):
+    """red_populate_disks: the disks of `specs` (DiskSpec list) generated on the
+    GPU; returns one System per spec."""
+    from .types import BMD, PARAM, VAR4, System
+    arr = (DiskSpec * len(specs))(*specs)
+    ns = [1 + s.n_pp + s.n_pl for s in specs]
+    tot = sum(ns)
+    r, v, p, md = np.zeros(tot, VAR4), np.zeros(tot, VAR4), np.zeros(tot, PARAM), np.zeros(tot, BMD)
+    playing = np.zeros((len(specs), 7), np.uint32)
+    _check(load().red_populate_disks(arr, len(specs), device, _p(playing), _p(r), _p(v), _p(p), _p(md)))
+    out, o = [], 0
+    for k, n in enumerate(ns):
+        sl = slice(o, o + n)
+        names = ["star"] + ["pp%d" % i for i in range(specs[k].n_pp)] + ["pl%d" % i for i in range(specs[k].n_pl)]
+        out.append(System(r[sl].copy(), v[sl].copy(), p[sl].copy(), md[sl].copy(), playing[k].copy(), names))
+        o += n
+    return out
 
 
 def mlp_param_count():
