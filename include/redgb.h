@@ -93,7 +93,8 @@ typedef struct {
     double threshold[RED_THRESHOLD_N]; /* parameter::threshold (parameter.cpp:214-237) */
     double output_interval;      /* dt_next is clamped to it after every step (main.cu:535-538); 0 = off */
     double length;               /* per-system integration length, code units (main.cu:471); 0 = unbounded */
-    int32_t gas_disk;            /* 0 none, 1 analytic (GAS_DISK_MODEL_ANALYTIC) */
+    int32_t gas_disk;            /* 0 none, 1 analytic (GAS_DISK_MODEL_ANALYTIC); 2 (FARGO) is refused with
+                                    RED_ERR_NOT_IMPLEMENTED: red's fargo_gas_disk cannot be constructed */
     red_gas_params_t gas;        /* after analytic_gas_disk::calc and transform_time */
     uint32_t event_capacity;     /* device event buffer, records; 0 = max(1024, total bodies) */
     int32_t device;              /* CUDA device ordinal */

@@ -77,6 +77,8 @@ extern "C" int red_calc_accel_noalloc(const red_accel_args_t* a)
     if (n > RED_NOALLOC_MAX_BODIES)
         return fail(RED_ERR_ARG, "red_calc_accel_noalloc: more bodies than RED_NOALLOC_MAX_BODIES");
     if (!a->r || !a->mass || !a->id || !a->accel) return fail(RED_ERR_ARG, "null device buffer");
+    if (a->gas_disk == 2) return fail(RED_ERR_NOT_IMPLEMENTED, "the FARGO gas disk cannot be constructed in red either");
+    if (a->gas_disk < 0 || a->gas_disk > 2) return fail(RED_ERR_ARG, "bad gas_disk");
     if (a->gas_disk && (!a->v || !a->radius || !a->density || !a->cd))
         return fail(RED_ERR_ARG, "gas drag needs v, radius, density and cd");
     if (a->precision < 0 || a->precision > 3) return fail(RED_ERR_ARG, "bad precision");

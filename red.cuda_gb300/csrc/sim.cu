@@ -546,6 +546,11 @@ void red_sim::create(const red_config_t* c, uint32_t n_systems, const uint32_t* 
                                                 "RUNGEKUTTAFEHLBERG78 are)"};
     }
     if (cfg.precision < 0 || cfg.precision > 3) throw ArgError{RED_ERR_ARG, "bad precision"};
+    // GAS_DISK_MODEL_FARGO: red's fargo_gas_disk constructor throws
+    // (transform_time "not yet implemented", fargo_gas_disk.cu:35, 259-261)
+    if (cfg.gas_disk == 2)
+        throw ArgError{RED_ERR_NOT_IMPLEMENTED, "the FARGO gas disk cannot be constructed in red either"};
+    if (cfg.gas_disk < 0 || cfg.gas_disk > 2) throw ArgError{RED_ERR_ARG, "bad gas_disk"};
     mode = cfg.precision;
     // FP64_EXACT combines the stages in red's order without FMA; the other
     // modes combine with FMA

@@ -215,7 +215,7 @@ class Sim:
     def __init__(self, systems, *, integrator="rkf78", adaptive=True, tolerance=1e-10, dt=None,
                  precision="mixed", stage_exact=False, collision_factor=0.0, ejection=0.0,
                  hit_centrum=0.0, gas=None, output_interval=0.0, length=0.0, error_check_for_tp=False,
-                 event_capacity=0, device=0, stream=None, t0=None):
+                 event_capacity=0, device=0, stream=None, t0=None, gas_model=None):
         L = load()
         if isinstance(systems, System):
             systems = [systems]
@@ -235,6 +235,8 @@ class Sim:
         if gas is not None:
             cfg.gas_disk = 1
             cfg.gas = gas_struct(gas)
+        if gas_model is not None:   # red's g_disk_model: 0 none, 1 analytic, 2 FARGO (refused)
+            cfg.gas_disk = int(gas_model)
         cfg.event_capacity = event_capacity
         cfg.device = device
         cfg.stream = stream

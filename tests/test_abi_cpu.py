@@ -65,7 +65,11 @@ def test_create_validates_inputs_before_touching_the_device(rg):
             assert e.code == code, (e, code)
         else:
             raise AssertionError("expected an error")
-    try:
-        rg.Sim(s, dt=0.1, integrator=3)     # no integrator of red has this code
-    except rg.RedError as e:
-        assert e.code == 6
+    for kw in (dict(integrator=3),      # no integrator of red has this code
+               dict(gas_model=2)):      # red's FARGO disk throws in its constructor
+        try:
+            rg.Sim(s, dt=0.1, **kw)
+        except rg.RedError as e:
+            assert e.code == 6, (kw, e)
+        else:
+            raise AssertionError("expected RED_ERR_NOT_IMPLEMENTED for %r" % kw)
