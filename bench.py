@@ -182,8 +182,9 @@ def roofline_for(rg, sim, systems, kw, peaks, traffic_per_launch):
             tot[int(k)] = tot.get(int(k), 0.0) + float(m)
             cnt[int(k)] = cnt.get(int(k), 0) + 1
         drain_events(sim)
-    names = {0: "stage", 1: "control", 2: "finish", 3: "collision", 4: "ejhc"}
+    names = {0: "stage", 1: "control", 2: "finish", 3: "collision", 4: "ejhc", 5: "proposer"}
     share = {names[k]: tot[k] / sum(tot.values()) for k in tot}
+    ms_by_kind = {names[k]: tot[k] / 5 for k in tot}   # ms per try of each kind (5 profiled tries)
     dom = max(tot, key=lambda k: tot[k])
     avg_ms = tot[dom] / cnt[dom]
     n_body = sum(s.n for s in systems)
@@ -207,7 +208,7 @@ def roofline_for(rg, sim, systems, kw, peaks, traffic_per_launch):
     out = {"kernel": names[dom], "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
            "frac": achieved / hbm, "traffic": traffic_per_launch.get(names[dom]), "avg_launch_ms": avg_ms,
            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback",
-           "share": share}
+           "share": share, "ms_per_try_by_kind": ms_by_kind}
     if names[dom] == "stage":
         # the same launch against the FP32 pipe: 20 FLOP per directed interaction
         tflops = 20.0 * sim.interactions_per_eval / (avg_ms * 1e-3) / 1e12
@@ -463,7 +464,8 @@ def run_ours(args, rg, rank, world, local_rank):
                 "sim_years_per_s": sim_years * world / (t_max * 1e-3),
                 "sim_years_per_s_plain": plain["sim_years_per_s"],
                 "ms_per_step_plain": plain["ms_per_step"],
-                "overhead_ms_per_try": t_max / args.steps - plain["ms_per_step"]}
+                "overhead_ms_per_try": t_max / args.steps - plain["ms_per_step"],
+                "kernels_ms_per_try": roof["ms_per_try_by_kind"].get("proposer")}
         print(json.dumps(line), flush=True)
     sim.close()
 

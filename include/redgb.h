@@ -191,7 +191,8 @@ int red_autotune(red_sim* sim);
 
 /* Runs one try launch by launch (outside the graph) with a CUDA event after
  * every kernel: ms[k] is the duration of launch k and kind[k] its kernel
- * (0 stage, 1 control, 2 finish, 3 collision, 4 ejection / hit-centrum).  The
+ * (0 stage, 1 control, 2 finish, 3 collision, 4 ejection / hit-centrum, 5 the
+ * learned proposer's two kernels, timed together).  The
  * try is a real one: the systems advance.  No counterpart in red; it stands in
  * for the per-launch cudaEvent timing of pp_disk::benchmark_calc_grav_accel
  * (pp_disk.cu:613-632). */

@@ -872,7 +872,7 @@ void red_sim::prep_positions()
 
 // One try of the integrator.  With kinds / evs set (profiling), an event is
 // recorded after every launch and the kernel kind noted: 0 stage, 1 control,
-// 2 finish, 3 collision, 4 ejection / hit-centrum.
+// 2 finish, 3 collision, 4 ejection / hit-centrum, 5 learned proposer.
 void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs)
 {
     int n = 0;
@@ -942,7 +942,10 @@ void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs
     launch_finish(F, (int)fsegs.size(), stream);
     mark(2);
     n++;
-    if (prop_on || log_on) enqueue_proposer(n);
+    if (prop_on || log_on) {
+        enqueue_proposer(n);
+        mark(5);
+    }
     if (coll) {
         CollParams Q;
         memset(&Q, 0, sizeof(Q));
