@@ -54,7 +54,7 @@ def kepler_E(ecc, mean, iters=30):
     for _ in range(iters):
         dE = (E - ecc * np.sin(E) - mean) / (1.0 - ecc * np.cos(E))
         E = E - dE
-        if np.max(np.abs(dE)) < 1e-15:
+        if np.max(np.abs(dE), initial=0.0) < 1e-15:
             break
     return E
 
