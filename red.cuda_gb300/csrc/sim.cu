@@ -165,16 +165,18 @@ static void gravity_classes(const SysInfo& si, int mode, GravClass out[3])
 }
 
 // Threads per sink group and sinks per group of one class: a power of two in
-// [4, 32] lanes.  Many sinks in the FP32 modes: 8 lanes serving 2 sinks each
-// (each source read feeds two interactions).  Few sinks: more lanes, the more
-// the longer the source list.
+// [4, 32] lanes.  Many sinks against more than 64 sources in the FP32 modes: 8
+// lanes serving 2 sinks each (each source read feeds two interactions).  A
+// short source list (a planetesimal class against a few protoplanets): 4 lanes
+// per sink, two butterfly rounds instead of three.  Few sinks: more lanes, the
+// more the longer the source list.
 static void class_shape(int mode, int nsink_all, int nsrc, int lanes_cap, int& lanes, int& spt)
 {
     const bool fp32 = (mode == MODE_MIXED || mode == MODE_FP32);
     lanes = 4;
     spt = 1;
     if (mode == MODE_FP64_EXACT) return;
-    if (fp32 && nsink_all >= 32 && lanes_cap >= 8) {
+    if (fp32 && nsink_all >= 32 && lanes_cap >= 8 && nsrc > 64) {
         lanes = 8;
         spt = 2;
         return;
