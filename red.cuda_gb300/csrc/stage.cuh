@@ -31,8 +31,8 @@ struct SmemStage {
         struct { float4 hi[2 * kTile]; float4 lo[2 * kTile]; } f;   // up to two tiles staged at once
         struct { D4 d[kTile]; int id[kTile]; } d;
     } src;
-    double acc[3 * kTile];          // per (sink, component) gravity sums
-    double sc[kTile][3];            // drag factor and gas velocity per sink
+    double acc[kTile];              // per (sink, component) gravity sums; per-thread record sums
+    double sc[32][3];               // drag factor and gas velocity per sink
     float4 star_hi[kStarBatch], star_lo[kStarBatch];   // the stars' double-single positions
     float2 star_m[kStarBatch];      // the stars' masses, double-single (0 for inactive stars)
     union {                         // the tile's sinks (cp.async in the prologue)
@@ -389,9 +389,14 @@ __device__ __forceinline__ void gravity_f64(SmemStage& sm, const StageParams& P,
 // (one instance per variant, for launches of many waves); VT = -1 takes it from
 // the launch argument, so that one kernel body serves all stages of a try and
 // stays in the instruction caches (launches of one wave, where the cold start
-// of each stage is on the critical path).
+// of each stage is on the critical path).  The per-variant instances run 7 CTAs
+// per SM (72 registers, 27 KB of shared memory each): their launches are many
+// waves of CTAs that each wait on a chain of memory round trips, and the seventh
+// CTA hides more of it (C4 ensemble stage -17 %, gas-drag disk -13 %, dense
+// -1.3 %; 8 CTAs at 64 registers spill and are slower).  The one-wave instance
+// keeps 80 registers.
 template <int MODE, bool EXACT, bool CL, int VT>
-__global__ void __launch_bounds__(kTile, 6) k_stage(const StageParams P, const int Vrt)
+__global__ void __launch_bounds__(kTile, VT >= 0 ? 7 : 6) k_stage(const StageParams P, const int Vrt)
 {
     constexpr bool kF32 = (MODE == MODE_MIXED || MODE == MODE_FP32);
     const int V = VT >= 0 ? VT : Vrt;

@@ -138,3 +138,23 @@ def test_ragged_ensemble_mixed(rg, monkeypatch, cluster):
         a, b = vec(st.r), vec(st1.r)
         scale = np.linalg.norm(b, axis=1).max() if len(b) > 1 else 1.0
         assert np.abs(a - b).max() <= 1e-12 * max(scale, 1e-300), k
+
+
+def test_persistent_ensemble_equals_single_systems(rg):
+    """An ensemble of more work items than one wave of CTAs holds (48 disks,
+    ~1500 items) runs the per-variant stage instances (7 CTAs per SM); alone,
+    each disk runs the one-wave instance that takes the variant as an argument.
+    FP64_EXACT, adaptive RKF7(8) through red_step (step quotas leave systems idle
+    for some tries): every disk ends bit for bit where it ends alone."""
+    rng = np.random.Generator(np.random.MT19937(21))
+    systems = [disk(rg, n_pp=int(rng.integers(0, 6)), n_pl=int(rng.integers(600, 1400)), seed=100 + k)
+               for k in range(48)]
+    systems[5] = disk(rg, n_pp=0, n_pl=0)   # a lone star: finished from the start
+    assert sum(s.n // 32 for s in systems) > 6 * 152
+    kw = dict(integrator="rkf78", adaptive=True, tolerance=1e-10, dt=1.0 * rg.ic.K, precision="fp64_exact",
+              stage_exact=True)
+    singles, together = run_alone_and_together(rg, systems, kw, 3)
+    for k, ((st1, i1), (st, i)) in enumerate(zip(singles, together)):
+        assert i.t == i1.t and i.n_tried == i1.n_tried, k
+        assert np.array_equal(vec(st.r), vec(st1.r)), k
+        assert np.array_equal(vec(st.v), vec(st1.v)), k
