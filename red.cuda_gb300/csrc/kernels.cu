@@ -446,12 +446,12 @@ __global__ void __launch_bounds__(kSegment) k_potential(const Segment* segs, con
 
 // ---------------------------------------------------------------------------
 // host transfers: one system's bodies between the device's structure of
-// arrays and the caller's records (var4_t r, v; param_t p; id and body type),
-// packed as rvp = [r: 4n | v: 4n | p: 4n] doubles and ib = [id, type] x n
+// arrays and the caller's records (var4_t r, v; param_t p: 4n doubles each,
+// one array per segment) and ib = [id, type] x n
 // ---------------------------------------------------------------------------
 __global__ void k_pack_state(int o, int n, const double* y_r, const double* y_v, const double* mass,
                              const double* radius, const double* density, const double* cd, const int* id,
-                             const int* btype, double* rvp, int* ib)
+                             const int* btype, StateSegs dst, int* ib)
 {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) {
@@ -460,19 +460,21 @@ __global__ void k_pack_state(int o, int n, const double* y_r, const double* y_v,
     }
     if (k >= 12LL * n) return;
     const int seg = (int)(k / (4LL * n));
+    double* out = dst.seg[seg];
+    if (!out) return;
     const int w = (int)(k - seg * 4LL * n);
     const int i = o + w / 4, c = w % 4;
     double v;
     if (seg == 0) v = c < 3 ? y_r[3 * i + c] : 0.0;
     else if (seg == 1) v = c < 3 ? y_v[3 * i + c] : 0.0;
     else v = c == 0 ? mass[i] : (c == 1 ? radius[i] : (c == 2 ? density[i] : cd[i]));
-    rvp[k] = v;
+    out[w] = v;
 }
 
 // Inverse of k_pack_state for the parts named in `what` (1 r, 2 v, 4 p, 8 id).
 // New positions also go to the FP32 copies of stage 0 (x, y, z; the .w words
 // follow mass and radius and are set by k_prep).
-__global__ void k_unpack_state(int o, int n, int what, const double* rvp, const int* ib, double* y_r, double* y_v,
+__global__ void k_unpack_state(int o, int n, int what, StateSegs src, const int* ib, double* y_r, double* y_v,
                                double* mass, double* radius, double* density, double* cd, int* id, float4* hi0,
                                float4* lo0)
 {
@@ -480,10 +482,10 @@ __global__ void k_unpack_state(int o, int n, int what, const double* rvp, const 
     if (k < n && (what & 8)) id[o + k] = ib[2 * k];
     if (k >= 12LL * n) return;
     const int seg = (int)(k / (4LL * n));
-    if (!(what & (1 << seg))) return;
+    if (!(what & (1 << seg)) || !src.seg[seg]) return;
     const int w = (int)(k - seg * 4LL * n);
     const int i = o + w / 4, c = w % 4;
-    const double v = rvp[k];
+    const double v = src.seg[seg][w];
     if (seg == 0) {
         if (c < 3) y_r[3 * i + c] = v;
         write_pos_c(hi0, lo0, i, c, v);
@@ -588,22 +590,22 @@ void launch_collide(const CollParams& P, int n_items, int n_segs, bool use_grid,
 }
 
 void launch_pack_state(int o, int n, const double* y_r, const double* y_v, const double* mass, const double* radius,
-                       const double* density, const double* cd, const int* id, const int* btype, double* rvp,
+                       const double* density, const double* cd, const int* id, const int* btype, StateSegs dst,
                        int* ib, cudaStream_t s)
 {
     if (n <= 0) return;
     const long long tot = 12LL * n;
     k_pack_state<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(o, n, y_r, y_v, mass, radius, density, cd, id, btype,
-                                                               rvp, ib);
+                                                               dst, ib);
 }
 
-void launch_unpack_state(int o, int n, int what, const double* rvp, const int* ib, double* y_r, double* y_v,
+void launch_unpack_state(int o, int n, int what, StateSegs src, const int* ib, double* y_r, double* y_v,
                          double* mass, double* radius, double* density, double* cd, int* id, float4* hi0,
                          float4* lo0, cudaStream_t s)
 {
     if (n <= 0) return;
     const long long tot = 12LL * n;
-    k_unpack_state<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(o, n, what, rvp, ib, y_r, y_v, mass, radius,
+    k_unpack_state<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(o, n, what, src, ib, y_r, y_v, mass, radius,
                                                                  density, cd, id, hi0, lo0);
 }
 

@@ -286,10 +286,17 @@ void launch_collision(const CollParams& P, int n_items, int n_segs, bool use_gri
 void launch_collide(const CollParams& P, int n_items, int n_segs, bool use_grid, cudaStream_t s);
 void launch_ejhc(const EjhcParams& P, int n_segs, cudaStream_t s);
 void launch_set_quota(DevSys* sys, int n_sys, int q, cudaStream_t s);
+// The three record arrays of red_get_state / red_set_state (r, v, p: 4 doubles
+// per body each).  Each is the device staging buffer or, when the caller's
+// array is pinned host memory, that array itself, read or written by the
+// kernel over the host link; a null entry is skipped.
+struct StateSegs {
+    double* seg[3];
+};
 void launch_pack_state(int o, int n, const double* y_r, const double* y_v, const double* mass, const double* radius,
-                       const double* density, const double* cd, const int* id, const int* btype, double* rvp,
+                       const double* density, const double* cd, const int* id, const int* btype, StateSegs dst,
                        int* ib, cudaStream_t s);
-void launch_unpack_state(int o, int n, int what, const double* rvp, const int* ib, double* y_r, double* y_v,
+void launch_unpack_state(int o, int n, int what, StateSegs src, const int* ib, double* y_r, double* y_v,
                          double* mass, double* radius, double* density, double* cd, int* id, float4* hi0,
                          float4* lo0, cudaStream_t s);
 void launch_potential(const Segment* segs, int n_segs, const SysInfo* sinfo, const double* y_r,

@@ -1663,6 +1663,20 @@ int red_calc_energy_interacting(red_sim* sim, uint32_t sys, double out[4])
 
 // Bytes of the transfer records of n bodies: r, v, p as 12 doubles, id and type as 2 ints.
 static size_t xfer_bytes(size_t n) { return n * (12 * sizeof(double) + 2 * sizeof(int)); }
+static_assert(sizeof(red_var4_t) == 4 * sizeof(double) && sizeof(red_param_t) == 4 * sizeof(double),
+              "the state records are 4 doubles each");
+
+// The device address of page-locked host memory (cudaHostAlloc / cudaHostRegister,
+// mapped into the device's address space), or null for any other pointer.
+static const void* device_view_of_host(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
 
 void red_sim::ensure_xfer(size_t bytes)
 {
@@ -1685,7 +1699,8 @@ void red_sim::pack_to_host(uint32_t s)
     ensure_xfer(xfer_bytes(n));
     double* rvp = (double*)d_xfer;
     int* ib = (int*)(d_xfer + 12 * n * sizeof(double));
-    launch_pack_state((int)h.off, (int)n, y_r, y_v, mass, radius, density, cd, id, btype, rvp, ib, stream);
+    launch_pack_state((int)h.off, (int)n, y_r, y_v, mass, radius, density, cd, id, btype,
+                      StateSegs{{rvp, rvp + 4 * n, rvp + 8 * n}}, ib, stream);
     CK(cudaGetLastError());
     launches++;
     CK(cudaMemcpyAsync(h_xfer, d_xfer, xfer_bytes(n), cudaMemcpyDeviceToHost, stream));
@@ -1698,21 +1713,34 @@ int red_get_state(red_sim* sim, uint32_t sys, red_var4_t* r, red_var4_t* v, red_
     if (int rc = check_sim(sim)) return rc;
     if (sys >= sim->n_sys) return set_error(RED_ERR_ARG, "bad system index");
     GUARD_BEGIN
-    // packed on the device, then copied straight into the caller's arrays (no
-    // staging copy on the host; pinned caller memory gets a direct DMA)
+    // packed on the device into the caller's arrays: pinned (page-locked) arrays
+    // directly by the kernel over the host link, others through the device
+    // staging buffer and one copy each (no staging copy on the host)
     const SysHost& h = sim->sh[sys];
     const size_t n = h.n;
     sim->ensure_xfer(xfer_bytes(n));
-    const double* d_rvp = (const double*)sim->d_xfer;
+    double* d_rvp = (double*)sim->d_xfer;
     const size_t ib_off = 12 * n * sizeof(double);
+    void* const out[3] = {r, v, p};
+    StateSegs dst{{nullptr, nullptr, nullptr}};
+    bool copy[3] = {false, false, false};
+    for (int k = 0; k < 3; k++) {
+        if (!out[k]) continue;
+        dst.seg[k] = (double*)device_view_of_host(out[k]);
+        if (!dst.seg[k]) {
+            dst.seg[k] = d_rvp + 4 * n * k;
+            copy[k] = true;
+        }
+    }
     launch_pack_state((int)h.off, (int)n, sim->y_r, sim->y_v, sim->mass, sim->radius, sim->density, sim->cd,
-                      sim->id, sim->btype, (double*)sim->d_xfer, (int*)(sim->d_xfer + ib_off), sim->stream);
+                      sim->id, sim->btype, dst, (int*)(sim->d_xfer + ib_off), sim->stream);
     CK(cudaGetLastError());
     sim->launches++;
+    for (int k = 0; k < 3; k++)   // var4_t and param_t are both 4 doubles
+        if (copy[k])
+            CK(cudaMemcpyAsync(out[k], d_rvp + 4 * n * k, n * sizeof(red_var4_t), cudaMemcpyDeviceToHost,
+                               sim->stream));
     const cudaMemcpyKind d2h = cudaMemcpyDeviceToHost;
-    if (r) CK(cudaMemcpyAsync(r, d_rvp, n * sizeof(red_var4_t), d2h, sim->stream));
-    if (v) CK(cudaMemcpyAsync(v, d_rvp + 4 * n, n * sizeof(red_var4_t), d2h, sim->stream));
-    if (p) CK(cudaMemcpyAsync(p, d_rvp + 8 * n, n * sizeof(red_param_t), d2h, sim->stream));
     if (md) CK(cudaMemcpyAsync(sim->h_xfer + ib_off, sim->d_xfer + ib_off, 2 * n * sizeof(int), d2h, sim->stream));
     CK(cudaStreamSynchronize(sim->stream));
     const int* ib = (const int*)(sim->h_xfer + ib_off);
@@ -1746,15 +1774,24 @@ int red_set_state(red_sim* sim, uint32_t sys, const red_var4_t* r, const red_var
             if (md[i].body_type != ib[2 * i + 1])
                 return set_error(RED_ERR_ARG, "body types cannot change through red_set_state");
     }
-    // the caller's arrays go straight to the device (no staging copy on the
-    // host; pinned caller memory gets a direct DMA); only the ids pass through
-    // the pinned staging buffer
+    // the caller's arrays go straight to the device: pinned (page-locked)
+    // arrays are read by the unpacking kernel over the host link, others are
+    // copied to the device staging buffer first (no staging copy on the host);
+    // only the ids pass through the pinned staging buffer
     double* d_rvp = (double*)sim->d_xfer;
     const cudaMemcpyKind h2d = cudaMemcpyHostToDevice;
+    const void* const in[3] = {r, v, p};
+    StateSegs src{{nullptr, nullptr, nullptr}};
     int what = 0;
-    if (r) { CK(cudaMemcpyAsync(d_rvp, r, n * sizeof(red_var4_t), h2d, sim->stream)); what |= 1; }
-    if (v) { CK(cudaMemcpyAsync(d_rvp + 4 * n, v, n * sizeof(red_var4_t), h2d, sim->stream)); what |= 2; }
-    if (p) { CK(cudaMemcpyAsync(d_rvp + 8 * n, p, n * sizeof(red_param_t), h2d, sim->stream)); what |= 4; }
+    for (int k = 0; k < 3; k++) {   // var4_t and param_t are both 4 doubles
+        if (!in[k]) continue;
+        what |= 1 << k;
+        src.seg[k] = (double*)device_view_of_host(in[k]);
+        if (!src.seg[k]) {
+            src.seg[k] = d_rvp + 4 * n * k;
+            CK(cudaMemcpyAsync(src.seg[k], in[k], n * sizeof(red_var4_t), h2d, sim->stream));
+        }
+    }
     if (md) {
         for (size_t i = 0; i < n; i++) {
             ib[2 * i] = md[i].id;
@@ -1764,7 +1801,7 @@ int red_set_state(red_sim* sim, uint32_t sys, const red_var4_t* r, const red_var
         CK(cudaMemcpyAsync(sim->d_xfer + ib_off, ib, 2 * n * sizeof(int), h2d, sim->stream));
         what |= 8;
     }
-    launch_unpack_state((int)h.off, (int)n, what, (const double*)sim->d_xfer,
+    launch_unpack_state((int)h.off, (int)n, what, src,
                         (const int*)(sim->d_xfer + 12 * n * sizeof(double)), sim->y_r, sim->y_v, sim->mass,
                         sim->radius, sim->density, sim->cd, sim->id, sim->pos_hi[0], sim->pos_lo[0], sim->stream);
     CK(cudaGetLastError());

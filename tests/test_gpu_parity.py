@@ -369,3 +369,48 @@ def test_collision_many_pairs_grid(rg, orc, factor):
         assert np.array_equal(mine["d"], ref["d"])
     assert len(ev) == n_ref
     assert n_ref > 50
+
+
+def pinned_copy(rg, s):
+    """A System whose r, v, p, md arrays live in page-locked host memory."""
+    torch = pytest.importorskip("torch")
+    out = rg.types.System(s.r.copy(), s.v.copy(), s.p.copy(), s.md.copy(), s.playing.copy())
+    keep = []
+    for f, t in (("r", rg.types.VAR4), ("v", rg.types.VAR4), ("p", rg.types.PARAM), ("md", rg.types.BMD)):
+        buf = torch.from_numpy(getattr(s, f).copy().view(np.uint8)).pin_memory()
+        keep.append(buf)
+        setattr(out, f, buf.numpy().view(t))
+    out._pinned = keep
+    return out
+
+
+def test_state_transfer_pinned_equals_pageable(rg):
+    """red_get_state / red_set_state read and write pinned caller arrays from the
+    kernel itself and pageable ones through the staging buffer: same bytes."""
+    s = small_disk(rg, n_pl=500, seed=4)
+    kw = dict(integrator="rkf78", adaptive=True, tolerance=1e-10, dt=1.0 * rg.ic.K, precision="mixed")
+    with rg.Sim(s, **kw) as sim:
+        for _ in range(3):
+            sim.step()
+        a = sim.get_state(0)
+        b = pinned_copy(rg, a)
+        for f in ("r", "v", "p", "md"):
+            getattr(b, f)[:] = 0
+        sim.get_state(0, out=b)
+        for f in ("r", "v", "p"):
+            assert getattr(a, f).tobytes() == getattr(b, f).tobytes(), f
+        for f in a.md.dtype.names:   # field by field: the records' padding is the caller's
+            assert np.array_equal(a.md[f], b.md[f]), f
+    moved = small_disk(rg, n_pl=500, seed=4)
+    moved.r["x"][5:40] += 1e-7
+    moved.v["y"][10:20] *= 1.0 + 1e-9
+    moved.p["radius"][30:50] *= 1.5
+    ends = []
+    for src in (moved, pinned_copy(rg, moved)):
+        with rg.Sim(s, **kw) as sim:
+            sim.set_state(0, src, parts="rvp")
+            for _ in range(3):
+                sim.step()
+            ends.append(sim.get_state(0))
+    for f in ("r", "v", "p"):
+        assert getattr(ends[0], f).tobytes() == getattr(ends[1], f).tobytes(), f
