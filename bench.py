@@ -14,8 +14,9 @@ error norm, step control, y_{n+1}, the collision check).
 Timing: CUDA events on the integration stream around each step, L2 flushed
 (a 256 MiB write) between timed steps; value = total interactions over all
 ranks / max over ranks of the summed step time.  `e2e` is the same metric
-through the C ABI with the state copied host->device before and
-device->host after every step (red_set_state / red_step / red_get_state).
+through the C ABI with the state of every system copied host->device before
+and device->host after every step (red_set_states / red_step /
+red_get_states, pinned host arrays).
 `--impl reference` times red's path on the host CPU: the oracle's
 restatement of red's code (the reference's own sources are not on the GPU
 host), with all host threads.
@@ -27,6 +28,7 @@ import subprocess
 import sys
 import threading
 import time
+import types
 
 import numpy as np
 
@@ -391,28 +393,27 @@ def run_ours(args, rg, rank, world, local_rank):
         traffic = {}
     roof = roofline_for(rg, sim, systems, kw, peaks, traffic)
 
-    # end to end through the C ABI with host buffers
-    import ctypes
-    n0 = systems[0].n
-    st = sim.get_state(0)
-    host = {f: torch.from_numpy(getattr(st, f).view(np.uint8)).pin_memory() for f in ("r", "v", "p", "md")}
+    # end to end through the C ABI with host buffers: the state of every system
+    # of the workload in and out each step
+    n_all = sim.bodies()
+    st = types.SimpleNamespace()
+    host = {}
+    for f, dt in (("r", rg.types.VAR4), ("v", rg.types.VAR4), ("p", rg.types.PARAM), ("md", rg.types.BMD)):
+        host[f] = torch.zeros(n_all * dt.itemsize, dtype=torch.uint8).pin_memory()
+        setattr(st, f, host[f].numpy().view(dt))
+    sim.get_states(st)
     e2e_steps = max(3, args.steps // 2)
-    st.r = host["r"].numpy().view(rg.types.VAR4)
-    st.v = host["v"].numpy().view(rg.types.VAR4)
-    st.p = host["p"].numpy().view(rg.types.PARAM)
-    st.md = host["md"].numpy().view(rg.types.BMD)
     torch.cuda.synchronize()
     rg.shard.barrier(local_rank)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        sim.set_state(0, st, parts="rv")      # inputs from pinned host memory
+        sim.set_states(st, parts="rv")      # inputs from pinned host memory
         sim.step()
-        sim.get_state(0, out=st, parts="rv")  # results into the same pinned buffers
+        sim.get_states(st, parts="rv")      # results into the same pinned buffers
     e2e_s = rg.shard.max_over_ranks(time.perf_counter() - t0, device="cuda")
     drain_events(sim)
-    tried_e2e = sim.info(0).n_tried
     e2e_value = ipe * ns * e2e_steps * world / e2e_s
-    bytes_state = n0 * (32 + 32)
+    bytes_state = n_all * (32 + 32)
 
     # the plain FP64 path on the same GPU, same workload (fewer steps)
     fp64 = None
@@ -445,7 +446,7 @@ def run_ours(args, rg, rank, world, local_rank):
                 "accept_fraction": (1.0 - failed / tried) if tried else None,
                 "e2e": {"value": e2e_value, "unit": "interactions/s", "h2d_bytes_per_step": bytes_state,
                         "d2h_bytes_per_step": bytes_state, "steps": e2e_steps,
-                        "api": "red_set_state(r, v) + red_step + red_get_state(r, v)"},
+                        "api": "red_set_states(r, v) + red_step + red_get_states(r, v), every system"},
                 "roofline": roof,
                 "cpu_baseline": cpu,
                 "plain_fp64_same_gpu": fp64,

@@ -177,6 +177,15 @@ int red_get_state(red_sim* sim, uint32_t sys, red_var4_t* r, red_var4_t* v, red_
                   red_body_metadata_t* md);
 int red_set_state(red_sim* sim, uint32_t sys, const red_var4_t* r, const red_var4_t* v,
                   const red_param_t* p, const red_body_metadata_t* md);
+/* The same for the systems [sys0, sys0 + count) at once: each array holds the
+ * systems' records one system after the other (the sum of their n_total).  One
+ * kernel and one synchronisation move an ensemble's state (no counterpart in
+ * red, which holds one system per process).  Null arrays are skipped; pinned
+ * (page-locked) arrays are read or written by the device directly. */
+int red_get_states(red_sim* sim, uint32_t sys0, uint32_t count, red_var4_t* r, red_var4_t* v, red_param_t* p,
+                   red_body_metadata_t* md);
+int red_set_states(red_sim* sim, uint32_t sys0, uint32_t count, const red_var4_t* r, const red_var4_t* v,
+                   const red_param_t* p, const red_body_metadata_t* md);
 int red_get_system_info(red_sim* sim, uint32_t sys, red_system_info_t* info);
 /* Sets dt_next of system sys (integrator::set_dt_next, integrator.h:24). */
 int red_set_dt_next(red_sim* sim, uint32_t sys, double dt_next);

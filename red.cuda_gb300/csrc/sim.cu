@@ -401,7 +401,7 @@ struct red_sim {
     char* h_xfer = nullptr;
     size_t xfer_cap = 0;
     void ensure_xfer(size_t bytes);
-    void pack_to_host(uint32_t s);
+    void pack_range_to_host(size_t o, size_t n);   // bodies [o, o + n) into h_xfer
     std::vector<double> grid_rmax;   // largest small-body radius the collision grid was planned for
     std::vector<double> star_mass;   // the first star's effective mass the plan was made with
     // learned step proposer (proposer.cu) and the feature log it is trained on
@@ -1692,14 +1692,12 @@ void red_sim::ensure_xfer(size_t bytes)
 }
 
 // System s's records, packed on the device and copied into h_xfer in one transfer.
-void red_sim::pack_to_host(uint32_t s)
+void red_sim::pack_range_to_host(size_t o, size_t n)
 {
-    const SysHost& h = sh[s];
-    const size_t n = h.n;
     ensure_xfer(xfer_bytes(n));
     double* rvp = (double*)d_xfer;
     int* ib = (int*)(d_xfer + 12 * n * sizeof(double));
-    launch_pack_state((int)h.off, (int)n, y_r, y_v, mass, radius, density, cd, id, btype,
+    launch_pack_state((int)o, (int)n, y_r, y_v, mass, radius, density, cd, id, btype,
                       StateSegs{{rvp, rvp + 4 * n, rvp + 8 * n}}, ib, stream);
     CK(cudaGetLastError());
     launches++;
@@ -1707,17 +1705,31 @@ void red_sim::pack_to_host(uint32_t s)
     CK(cudaStreamSynchronize(stream));
 }
 
-int red_get_state(red_sim* sim, uint32_t sys, red_var4_t* r, red_var4_t* v, red_param_t* p,
-                  red_body_metadata_t* md)
+// Systems [s0, s0 + cnt) whose body ranges follow each other on the device
+// (always, until a compaction leaves a system's tail unused).
+static bool contiguous(const red_sim* sim, uint32_t s0, uint32_t cnt)
 {
-    if (int rc = check_sim(sim)) return rc;
-    if (sys >= sim->n_sys) return set_error(RED_ERR_ARG, "bad system index");
-    GUARD_BEGIN
-    // packed on the device into the caller's arrays: pinned (page-locked) arrays
-    // directly by the kernel over the host link, others through the device
-    // staging buffer and one copy each (no staging copy on the host)
-    const SysHost& h = sim->sh[sys];
-    const size_t n = h.n;
+    for (uint32_t s = s0 + 1; s < s0 + cnt; s++)
+        if (sim->sh[s].off != sim->sh[s - 1].off + sim->sh[s - 1].n) return false;
+    return true;
+}
+
+static size_t bodies_in(const red_sim* sim, uint32_t s0, uint32_t cnt)
+{
+    size_t n = 0;
+    for (uint32_t s = s0; s < s0 + cnt; s++) n += sim->sh[s].n;
+    return n;
+}
+
+// The records of systems [s0, s0 + cnt), contiguous on the device, packed on
+// the device into the caller's arrays: pinned (page-locked) arrays directly by
+// the kernel over the host link, others through the device staging buffer and
+// one copy each (no staging copy on the host).
+static void get_state_range(red_sim* sim, uint32_t s0, uint32_t cnt, red_var4_t* r, red_var4_t* v, red_param_t* p,
+                            red_body_metadata_t* md)
+{
+    const size_t o = sim->sh[s0].off;
+    const size_t n = bodies_in(sim, s0, cnt);
     sim->ensure_xfer(xfer_bytes(n));
     double* d_rvp = (double*)sim->d_xfer;
     const size_t ib_off = 12 * n * sizeof(double);
@@ -1732,54 +1744,82 @@ int red_get_state(red_sim* sim, uint32_t sys, red_var4_t* r, red_var4_t* v, red_
             copy[k] = true;
         }
     }
-    launch_pack_state((int)h.off, (int)n, sim->y_r, sim->y_v, sim->mass, sim->radius, sim->density, sim->cd,
-                      sim->id, sim->btype, dst, (int*)(sim->d_xfer + ib_off), sim->stream);
+    launch_pack_state((int)o, (int)n, sim->y_r, sim->y_v, sim->mass, sim->radius, sim->density, sim->cd, sim->id,
+                      sim->btype, dst, (int*)(sim->d_xfer + ib_off), sim->stream);
     CK(cudaGetLastError());
     sim->launches++;
     for (int k = 0; k < 3; k++)   // var4_t and param_t are both 4 doubles
         if (copy[k])
             CK(cudaMemcpyAsync(out[k], d_rvp + 4 * n * k, n * sizeof(red_var4_t), cudaMemcpyDeviceToHost,
                                sim->stream));
-    const cudaMemcpyKind d2h = cudaMemcpyDeviceToHost;
-    if (md) CK(cudaMemcpyAsync(sim->h_xfer + ib_off, sim->d_xfer + ib_off, 2 * n * sizeof(int), d2h, sim->stream));
+    if (md)
+        CK(cudaMemcpyAsync(sim->h_xfer + ib_off, sim->d_xfer + ib_off, 2 * n * sizeof(int), cudaMemcpyDeviceToHost,
+                           sim->stream));
     CK(cudaStreamSynchronize(sim->stream));
     const int* ib = (const int*)(sim->h_xfer + ib_off);
     if (md) {
         for (size_t i = 0; i < n; i++) {
             md[i].id = ib[2 * i];
             md[i].body_type = ib[2 * i + 1];
-            md[i].mig_type = sim->mig_type[h.off + i];
-            md[i].mig_stop_at = sim->mig_stop_at[h.off + i];
+            md[i].mig_type = sim->mig_type[o + i];
+            md[i].mig_stop_at = sim->mig_stop_at[o + i];
         }
     }
-    return RED_OK;
-    GUARD_END
 }
 
-int red_set_state(red_sim* sim, uint32_t sys, const red_var4_t* r, const red_var4_t* v, const red_param_t* p,
-                  const red_body_metadata_t* md)
+static void get_states(red_sim* sim, uint32_t s0, uint32_t cnt, red_var4_t* r, red_var4_t* v, red_param_t* p,
+                       red_body_metadata_t* md)
+{
+    sim->ensure_xfer(xfer_bytes(bodies_in(sim, s0, cnt)));   // no reallocation between the ranges
+    if (contiguous(sim, s0, cnt)) {
+        get_state_range(sim, s0, cnt, r, v, p, md);
+        return;
+    }
+    size_t a = 0;
+    for (uint32_t s = s0; s < s0 + cnt; s++) {
+        get_state_range(sim, s, 1, r ? r + a : nullptr, v ? v + a : nullptr, p ? p + a : nullptr,
+                        md ? md + a : nullptr);
+        a += sim->sh[s].n;
+    }
+}
+
+int red_get_state(red_sim* sim, uint32_t sys, red_var4_t* r, red_var4_t* v, red_param_t* p,
+                  red_body_metadata_t* md)
 {
     if (int rc = check_sim(sim)) return rc;
     if (sys >= sim->n_sys) return set_error(RED_ERR_ARG, "bad system index");
     GUARD_BEGIN
-    const SysHost& h = sim->sh[sys];
-    const size_t n = h.n;
+    get_states(sim, sys, 1, r, v, p, md);
+    return RED_OK;
+    GUARD_END
+}
+
+int red_get_states(red_sim* sim, uint32_t sys0, uint32_t count, red_var4_t* r, red_var4_t* v, red_param_t* p,
+                   red_body_metadata_t* md)
+{
+    if (int rc = check_sim(sim)) return rc;
+    if (count == 0 || sys0 >= sim->n_sys || count > sim->n_sys - sys0)
+        return set_error(RED_ERR_ARG, "bad system range");
+    GUARD_BEGIN
+    get_states(sim, sys0, count, r, v, p, md);
+    return RED_OK;
+    GUARD_END
+}
+
+// The caller's records of systems [s0, s0 + cnt), contiguous on the device, to
+// the device.  Pinned (page-locked) arrays are read by the unpacking kernel over
+// the host link, others are copied to the device staging buffer first (no
+// staging copy on the host); only the ids pass through the pinned staging
+// buffer.  Returns whether the plan must be rebuilt.
+static bool set_state_range(red_sim* sim, uint32_t s0, uint32_t cnt, const red_var4_t* r, const red_var4_t* v,
+                            const red_param_t* p, const red_body_metadata_t* md)
+{
+    const size_t o = sim->sh[s0].off;
+    const size_t n = bodies_in(sim, s0, cnt);
     sim->ensure_xfer(xfer_bytes(n));
     const size_t ib_off = 12 * n * sizeof(double);
     int* ib = (int*)(sim->h_xfer + ib_off);
-    if (md) {
-        // body types are fixed by the class ranges: read the current ones first
-        sim->pack_to_host(sys);
-        for (size_t i = 0; i < n; i++)
-            if (md[i].body_type != ib[2 * i + 1])
-                return set_error(RED_ERR_ARG, "body types cannot change through red_set_state");
-    }
-    // the caller's arrays go straight to the device: pinned (page-locked)
-    // arrays are read by the unpacking kernel over the host link, others are
-    // copied to the device staging buffer first (no staging copy on the host);
-    // only the ids pass through the pinned staging buffer
     double* d_rvp = (double*)sim->d_xfer;
-    const cudaMemcpyKind h2d = cudaMemcpyHostToDevice;
     const void* const in[3] = {r, v, p};
     StateSegs src{{nullptr, nullptr, nullptr}};
     int what = 0;
@@ -1789,33 +1829,72 @@ int red_set_state(red_sim* sim, uint32_t sys, const red_var4_t* r, const red_var
         src.seg[k] = (double*)device_view_of_host(in[k]);
         if (!src.seg[k]) {
             src.seg[k] = d_rvp + 4 * n * k;
-            CK(cudaMemcpyAsync(src.seg[k], in[k], n * sizeof(red_var4_t), h2d, sim->stream));
+            CK(cudaMemcpyAsync(src.seg[k], in[k], n * sizeof(red_var4_t), cudaMemcpyHostToDevice, sim->stream));
         }
     }
     if (md) {
         for (size_t i = 0; i < n; i++) {
             ib[2 * i] = md[i].id;
-            sim->mig_type[h.off + i] = md[i].mig_type;
-            sim->mig_stop_at[h.off + i] = md[i].mig_stop_at;
+            sim->mig_type[o + i] = md[i].mig_type;
+            sim->mig_stop_at[o + i] = md[i].mig_stop_at;
         }
-        CK(cudaMemcpyAsync(sim->d_xfer + ib_off, ib, 2 * n * sizeof(int), h2d, sim->stream));
+        CK(cudaMemcpyAsync(sim->d_xfer + ib_off, ib, 2 * n * sizeof(int), cudaMemcpyHostToDevice, sim->stream));
         what |= 8;
     }
-    launch_unpack_state((int)h.off, (int)n, what, src,
-                        (const int*)(sim->d_xfer + 12 * n * sizeof(double)), sim->y_r, sim->y_v, sim->mass,
-                        sim->radius, sim->density, sim->cd, sim->id, sim->pos_hi[0], sim->pos_lo[0], sim->stream);
+    launch_unpack_state((int)o, (int)n, what, src, (const int*)(sim->d_xfer + ib_off), sim->y_r, sim->y_v,
+                        sim->mass, sim->radius, sim->density, sim->cd, sim->id, sim->pos_hi[0], sim->pos_lo[0],
+                        sim->stream);
     CK(cudaGetLastError());
     sim->launches++;
-    bool replan = false;
+    bool replan = md != nullptr;   // ids decide which bodies act as sources
     if (p) {
         // the collision grid's cells must stay wider than the largest collision distance,
         // and the work items carry the first star's mass
-        double rmax = 0.0;
-        for (size_t k = h.n_SI(); k < n; k++) rmax = std::max(rmax, p[k].radius);
-        replan = rmax > sim->grid_rmax[sys];
-        if (h.playing[0] > 0 && p[0].mass != sim->star_mass[sys]) replan = true;
+        size_t a = 0;
+        for (uint32_t s = s0; s < s0 + cnt; s++) {
+            const SysHost& h = sim->sh[s];
+            double rmax = 0.0;
+            for (size_t k = h.n_SI(); k < h.n; k++) rmax = std::max(rmax, p[a + k].radius);
+            if (rmax > sim->grid_rmax[s]) replan = true;
+            if (h.playing[0] > 0 && p[a].mass != sim->star_mass[s]) replan = true;
+            a += h.n;
+        }
     }
-    if (md) replan = true;   // ids decide which bodies act as sources
+    return replan;
+}
+
+// Body types are fixed by the class ranges: the new metadata of systems
+// [s0, s0 + cnt) must keep the current ones (checked before anything is written).
+static void check_body_types(red_sim* sim, uint32_t s0, uint32_t cnt, const red_body_metadata_t* md)
+{
+    size_t a = 0;
+    for (uint32_t s = s0; s < s0 + cnt; s++) {
+        const size_t n = sim->sh[s].n;
+        sim->pack_range_to_host(sim->sh[s].off, n);
+        const int* ib = (const int*)(sim->h_xfer + 12 * n * sizeof(double));
+        for (size_t i = 0; i < n; i++)
+            if (md[a + i].body_type != ib[2 * i + 1])
+                throw ArgError{RED_ERR_ARG, "body types cannot change through red_set_state"};
+        a += n;
+    }
+}
+
+static void set_states(red_sim* sim, uint32_t s0, uint32_t cnt, const red_var4_t* r, const red_var4_t* v,
+                       const red_param_t* p, const red_body_metadata_t* md)
+{
+    bool replan = false;
+    sim->ensure_xfer(xfer_bytes(bodies_in(sim, s0, cnt)));   // no reallocation between the ranges
+    if (md) check_body_types(sim, s0, cnt, md);
+    if (contiguous(sim, s0, cnt)) {
+        replan = set_state_range(sim, s0, cnt, r, v, p, md);
+    } else {
+        size_t a = 0;
+        for (uint32_t s = s0; s < s0 + cnt; s++) {
+            replan |= set_state_range(sim, s, 1, r ? r + a : nullptr, v ? v + a : nullptr, p ? p + a : nullptr,
+                                      md ? md + a : nullptr);
+            a += sim->sh[s].n;
+        }
+    }
     if (replan) {
         CK(cudaStreamSynchronize(sim->stream));
         sim->build_plan();
@@ -1823,7 +1902,29 @@ int red_set_state(red_sim* sim, uint32_t sys, const red_var4_t* r, const red_var
     // new positions alone are already in the FP32 copies (k_unpack_state);
     // masses, radii and ids change their .w words
     if (p || md || replan) sim->prep_positions();
+    // the unpacking kernel reads pinned caller arrays: done before they may be reused
     CK(cudaStreamSynchronize(sim->stream));
+}
+
+int red_set_state(red_sim* sim, uint32_t sys, const red_var4_t* r, const red_var4_t* v, const red_param_t* p,
+                  const red_body_metadata_t* md)
+{
+    if (int rc = check_sim(sim)) return rc;
+    if (sys >= sim->n_sys) return set_error(RED_ERR_ARG, "bad system index");
+    GUARD_BEGIN
+    set_states(sim, sys, 1, r, v, p, md);
+    return RED_OK;
+    GUARD_END
+}
+
+int red_set_states(red_sim* sim, uint32_t sys0, uint32_t count, const red_var4_t* r, const red_var4_t* v,
+                   const red_param_t* p, const red_body_metadata_t* md)
+{
+    if (int rc = check_sim(sim)) return rc;
+    if (count == 0 || sys0 >= sim->n_sys || count > sim->n_sys - sys0)
+        return set_error(RED_ERR_ARG, "bad system range");
+    GUARD_BEGIN
+    set_states(sim, sys0, count, r, v, p, md);
     return RED_OK;
     GUARD_END
 }

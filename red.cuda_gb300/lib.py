@@ -24,7 +24,7 @@ INTEGRATOR = {"euler": 0, "e": 0, "rk2": 1, "rk4": 2, "rkf78": 4, "rkf8": 4}
 EXPORTS = ["red_create", "red_destroy", "red_step", "red_launch_tries", "red_synchronize",
            "red_handle_events", "red_check_for_collision", "red_check_for_ejection_hit_centrum",
            "red_calc_dydx", "red_calc_integral", "red_calc_energy_interacting", "red_get_state",
-           "red_set_state", "red_get_system_info", "red_set_dt_next", "red_rebuild_vectors",
+           "red_set_state", "red_get_states", "red_set_states", "red_get_system_info", "red_set_dt_next", "red_rebuild_vectors",
            "red_autotune", "red_profile_try", "red_interactions_per_eval", "red_kernel_launches", "red_n_systems",
            "red_n_bodies",
            "red_calc_accel_noalloc", "red_mlp_param_count", "red_mlp_predict", "red_mlp_grad", "red_mlp_adam",
@@ -123,6 +123,8 @@ def load(path=LIB_PATH):
     L.red_calc_energy_interacting.argtypes = [P, C.c_uint32, P]
     L.red_get_state.argtypes = [P, C.c_uint32, P, P, P, P]
     L.red_set_state.argtypes = [P, C.c_uint32, P, P, P, P]
+    L.red_get_states.argtypes = [P, C.c_uint32, C.c_uint32, P, P, P, P]
+    L.red_set_states.argtypes = [P, C.c_uint32, C.c_uint32, P, P, P, P]
     L.red_get_system_info.argtypes = [P, C.c_uint32, C.POINTER(SystemInfo)]
     L.red_set_dt_next.argtypes = [P, C.c_uint32, C.c_double]
     L.red_rebuild_vectors.argtypes = [P]
@@ -154,6 +156,13 @@ def load(path=LIB_PATH):
 
 def _p(a):
     return a.ctypes.data_as(C.c_void_p)
+
+
+def _check_out(a, dtype, n):
+    """An array the library writes n records of `dtype` into: contiguous, of
+    that exact layout (a packed copy of a padded record would be overrun)."""
+    if not a.flags["C_CONTIGUOUS"] or len(a) != n or a.dtype != dtype or a.dtype.itemsize != dtype.itemsize:
+        raise ValueError("out arrays must be contiguous with %d records of %s" % (n, dtype))
 
 
 def _check(rc):
@@ -340,9 +349,8 @@ class Sim:
         else:
             n = load().red_n_bodies(self.h, sys)
             r, v, p, md = out.r, out.v, out.p, out.md
-            for a in (r, v, p, md):
-                if not a.flags["C_CONTIGUOUS"] or len(a) != n:
-                    raise ValueError("out arrays must be contiguous with %d records" % n)
+            for a, t in ((r, VAR4), (v, VAR4), (p, PARAM), (md, BMD)):
+                _check_out(a, t, n)
         ptr = [_p(a) if k in parts else None for a, k in ((r, "r"), (v, "v"), (p, "p"), (md, "m"))]
         _check(load().red_get_state(self.h, sys, *ptr))
         if out is not None:
@@ -357,6 +365,36 @@ class Sim:
         arrs = [(s.r, VAR4, "r"), (s.v, VAR4, "v"), (s.p, PARAM, "p"), (s.md, BMD, "m")]
         keep = [np.ascontiguousarray(a, t) if k in parts else None for a, t, k in arrs]
         _check(load().red_set_state(self.h, sys, *[_p(a) if a is not None else None for a in keep]))
+
+    def bodies(self, sys0=0, count=None):
+        """Bodies of the systems [sys0, sys0 + count) (all from sys0 by default)."""
+        count = self.n_systems - sys0 if count is None else count
+        return sum(int(load().red_n_bodies(self.h, k)) for k in range(sys0, sys0 + count))
+
+    def get_states(self, out, sys0=0, count=None, parts="rvpm"):
+        """The records of systems [sys0, sys0 + count), one system after the other,
+        into out's arrays (a System or any object with contiguous r, v, p, md of
+        bodies(sys0, count) records) in one call; returns out."""
+        count = self.n_systems - sys0 if count is None else count
+        n = self.bodies(sys0, count)
+        arrs = [(out.r, "r"), (out.v, "v"), (out.p, "p"), (out.md, "m")]
+        for (a, k), t in zip(arrs, (VAR4, VAR4, PARAM, BMD)):
+            if k in parts:
+                _check_out(a, t, n)
+        _check(load().red_get_states(self.h, sys0, count, *[_p(a) if k in parts else None for a, k in arrs]))
+        return out
+
+    def set_states(self, s, sys0=0, count=None, parts="rvpm"):
+        """Writes the arrays of s named in `parts` (the records of systems
+        [sys0, sys0 + count), one system after the other) in one call."""
+        count = self.n_systems - sys0 if count is None else count
+        n = self.bodies(sys0, count)
+        arrs = [(s.r, VAR4, "r"), (s.v, VAR4, "v"), (s.p, PARAM, "p"), (s.md, BMD, "m")]
+        keep = [np.ascontiguousarray(a, t) if k in parts else None for a, t, k in arrs]
+        for a in keep:
+            if a is not None and len(a) != n:
+                raise ValueError("arrays must hold %d records" % n)
+        _check(load().red_set_states(self.h, sys0, count, *[_p(a) if a is not None else None for a in keep]))
 
     def set_dt_next(self, sys, dt):
         _check(load().red_set_dt_next(self.h, sys, dt))

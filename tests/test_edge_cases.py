@@ -158,3 +158,95 @@ def test_persistent_ensemble_equals_single_systems(rg):
         assert i.t == i1.t and i.n_tried == i1.n_tried, k
         assert np.array_equal(vec(st.r), vec(st1.r)), k
         assert np.array_equal(vec(st.v), vec(st1.v)), k
+
+
+def concat(states):
+    # dtype= keeps red's record layout (a plain concatenate packs the metadata's padding away)
+    return {f: np.concatenate([getattr(st, f) for st in states], dtype=getattr(states[0], f).dtype)
+            for f in ("r", "v", "p", "md")}
+
+
+class Records:
+    def __init__(self, d):
+        self.r, self.v, self.p, self.md = d["r"], d["v"], d["p"], d["md"]
+
+
+def pinned_records(d):
+    torch = pytest.importorskip("torch")
+    out = {}
+    for f, a in d.items():
+        buf = torch.zeros(a.nbytes, dtype=torch.uint8).pin_memory()
+        out[f] = buf.numpy().view(a.dtype)
+        out[f][...] = a
+        out[f + "_buf"] = buf
+    return Records(out)
+
+
+def same_records(a, b):
+    for f in ("r", "v", "p"):
+        assert getattr(a, f).tobytes() == getattr(b, f).tobytes(), f
+    for f in a.md.dtype.names:
+        assert np.array_equal(a.md[f], b.md[f]), f
+
+
+def batched_setup(rg, holes):
+    """A ragged ensemble; with holes, two disks whose collisions merge bodies
+    and a compaction that shortens them (their device ranges then no longer
+    follow each other)."""
+    kw = dict(integrator="rkf78", adaptive=True, tolerance=1e-10, dt=1.0 * rg.ic.K, precision="mixed")
+    if not holes:
+        return ragged(rg)[1:], kw, lambda sim: None
+    from test_gpu_parity import collide_disk
+    systems = [collide_disk(rg), disk(rg, n_pp=2, n_pl=150, seed=8), collide_disk(rg), disk(rg, n_pp=1, n_pl=90)]
+    kw = dict(integrator="rk4", adaptive=False, dt=0.5 * rg.ic.K, precision="mixed", collision_factor=1.0)
+
+    def merge(sim):
+        sim.launch_tries(1)
+        sim.synchronize()
+        sim.handle_events()
+        sim.rebuild_vectors()
+    return systems, kw, merge
+
+
+@pytest.mark.parametrize("holes", [False, True])
+def test_batched_state_calls(rg, holes):
+    """red_get_states / red_set_states over an ensemble equal the per-system
+    calls, into pageable and pinned arrays; with holes the calls go system by
+    system."""
+    systems, kw, prepare = batched_setup(rg, holes)
+    fields = ("r", "v", "p", "md")
+    with rg.Sim(systems, **kw) as sim:
+        prepare(sim)
+        if holes:
+            assert sim.info(0).n_total < systems[0].n and sim.info(2).n_total < systems[2].n
+        sim.step()
+        n = sim.bodies()
+        per = Records(concat([sim.get_state(k) for k in range(sim.n_systems)]))
+        assert len(per.r) == n
+        same_records(per, sim.get_states(Records({f: np.zeros_like(getattr(per, f)) for f in fields})))
+        same_records(per, sim.get_states(pinned_records({f: np.zeros_like(getattr(per, f)) for f in fields})))
+        lo, m = sim.bodies(0, 1), sim.bodies(1, 2)
+        part = sim.get_states(Records({f: np.zeros_like(getattr(per, f)[:m]) for f in fields}), sys0=1, count=2)
+        same_records(Records({f: getattr(per, f)[lo:lo + m] for f in fields}), part)
+        moved = Records({f: getattr(per, f).copy() for f in fields})
+        moved.r["x"] += 1e-9
+        moved.v["z"] *= 1.0 + 1e-9
+    ends = []
+    for how in ("per-system", "batched", "batched-pinned"):
+        with rg.Sim(systems, **kw) as sim:
+            prepare(sim)
+            sim.step()
+            if how == "per-system":
+                a = 0
+                for k in range(sim.n_systems):
+                    m = sim.bodies(k, 1)
+                    sim.set_state(k, Records({f: getattr(moved, f)[a:a + m] for f in fields}), parts="rv")
+                    a += m
+            elif how == "batched":
+                sim.set_states(moved, parts="rv")
+            else:
+                sim.set_states(pinned_records({f: getattr(moved, f) for f in fields}), parts="rv")
+            sim.step()
+            ends.append(sim.get_states(Records({f: np.zeros_like(getattr(per, f)) for f in fields})))
+    same_records(ends[0], ends[1])
+    same_records(ends[0], ends[2])
