@@ -234,7 +234,8 @@ static __device__ double gas_reduction_factor(const GasDev& g, double t)
 }
 
 // Drag factor f and gas velocity (gx, gy, 0) at (r, v): the acceleration is
-// f (v_gas - v) (calc_drag_accel_NSI, pp_disk.cu:485-521).
+// f (v_gas - v) (calc_drag_accel_NSI, pp_disk.cu:485-521).  red's FP64
+// arithmetic, for the FP64 modes.
 static __device__ void drag_factor(const GasDev& g, double decr, double m_star, double rx, double ry, double rz, double vx,
                             double vy, double vz, double cd, double radius, double density, double& f, double& gx,
                             double& gy)
@@ -274,6 +275,42 @@ static __device__ void drag_factor(const GasDev& g, double decr, double m_star, 
     const double ux = gx - vx, uy = gy - vy, uz = 0.0 - vz;
     const double un = sqrt(ux * ux + uy * uy + uz * uz);
     f = decr * (3.0 * cd * dens * un) / (8.0 * radius * density);
+}
+
+// The same drag for the FP32 modes, with the transcendental factors in FP32.
+// GB300 runs FP64 at 1/64 of the FP32 rate: red's chain of one sink (three
+// pow, an exp, five square roots, three divisions) held a warp for ~9 us of
+// every tile.  The gas velocity stays FP64, as vc fv (-y, x) / r (the vector
+// red's branches form), because v_gas - v cancels ~99.5 % of it; fv = 1 + d,
+// d = -x / (1 + sqrt(1 - x)) for x = 2 eta r^p, keeps it to ~1e-10.  The
+// factor f (gas density, |v_gas - v|, the body's cross-section) is FP32, a
+// ~1e-6 relative error on a drag that is at most ~1e-5 of a body's
+// acceleration in red's disks, below the modes' own FP32 pair error.
+static __device__ void drag_factor_fast(const GasDev& g, double decr, double m_star, double rx, double ry, double rz,
+                                        double vx, double vy, double vz, double cd, double radius, double density,
+                                        double& f, double& gx, double& gy)
+{
+    const double r2 = rx * rx + ry * ry;   // 0 on the disk's axis: NaN drag, as red's pow(0, p < 0)
+    const double ir = rsqrt(r2);
+    const float r = (float)(r2 * ir);
+    const float x = 2.0f * (float)g.eta[0] * powf(r, (float)g.eta[1]);
+    const double fv = 1.0 + (double)(-x / (1.0f + sqrtf(1.0f - x)));
+    const double s = sqrt(m_star * ir) * ir * fv;
+    gx = -ry * s;
+    gy = rx * s;
+    const float h = (float)g.sch[0] * powf(r, (float)g.sch[1]);
+    const float zh = (float)rz / h;
+    const float arg = zh * zh;
+    float dens;
+    if (0.1f < r) {
+        dens = (float)g.rho[0] * powf(r, (float)g.rho[1]) * expf(-arg);
+    } else {
+        const float a = (float)g.rho[0] * powf(0.1f, (float)g.rho[1] - 4.0f);
+        dens = a * (r * r) * (r * r) * expf(-arg);
+    }
+    const double ux = gx - vx, uy = gy - vy, uz = -vz;
+    const float un = sqrtf((float)(ux * ux + uy * uy + uz * uz));
+    f = decr * (double)((3.0f * (float)cd * dens * un) / (8.0f * (float)radius * (float)density));
 }
 
 struct alignas(32) D4 {

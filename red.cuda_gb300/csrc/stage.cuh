@@ -538,9 +538,14 @@ __global__ void __launch_bounds__(kTile, VT >= 0 ? 7 : 6) k_stage(const StagePar
     if (drag_act && t < it.nsink) {
         const int ib = it.sink0 + t;
         double f, gx, gy;
-        drag_factor(P.gas, decr, P.mass[it.soff], P.r_in[3 * ib], P.r_in[3 * ib + 1], P.r_in[3 * ib + 2],
-                    P.Kr[s][3 * ib], P.Kr[s][3 * ib + 1], P.Kr[s][3 * ib + 2], P.cd[ib], P.radius[ib], P.density[ib],
-                    f, gx, gy);
+        const double* rb = P.r_in + 3 * ib;
+        const double* vb = P.Kr[s] + 3 * ib;
+        if constexpr (kF32)
+            drag_factor_fast(P.gas, decr, P.mass[it.soff], rb[0], rb[1], rb[2], vb[0], vb[1], vb[2], P.cd[ib],
+                             P.radius[ib], P.density[ib], f, gx, gy);
+        else
+            drag_factor(P.gas, decr, P.mass[it.soff], rb[0], rb[1], rb[2], vb[0], vb[1], vb[2], P.cd[ib],
+                        P.radius[ib], P.density[ib], f, gx, gy);
         sm.sc[t][0] = f;
         sm.sc[t][1] = gx;
         sm.sc[t][2] = gy;

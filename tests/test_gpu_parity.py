@@ -111,6 +111,34 @@ def test_drag(rg, orc):
     assert np.abs(ref[nsi:] - vec(grav)[nsi:]).max() > 0.0   # drag acts
 
 
+def test_drag_mixed(rg, orc):
+    """MIXED evaluates the drag factor in FP32.  The drag part of the
+    acceleration (with the gas disk minus without) follows the oracle's to
+    1e-5 of itself plus the rounding of the sum (4e-16 of the acceleration);
+    the drag is at most ~1e-5 of a body's acceleration here, so the whole
+    acceleration keeps the mode's 1e-9."""
+    s = rg.ic.config3(n_pp=3, n_pl=200, seed=5)
+    keys = rg.ic.gas_disk_config3()
+    keys["time_dependence"] = "exponential"
+    keys["t0"] = 0.5
+    keys["e_folding_time"] = 3.0
+    gas = np.array([rg.ic.gas_params(keys)], dtype=rg.types.GAS)
+    t = 1.25 * 365.25 * rg.ic.K
+    with rg.Sim(s, dt=0.01, precision="mixed", gas=gas[0]) as sim:
+        a = vec(sim.calc_dydx(0, 1, t))
+    with rg.Sim(s, dt=0.01, precision="mixed") as sim:
+        a0 = vec(sim.calc_dydx(0, 1, t))
+    rc, ref = orc.calc_dydx(obody(orc, s), 1, t, gas=np.ascontiguousarray(gas, dtype=orc.GAS), sem=orc.SEM_GPU)
+    ref = vec(ref)
+    _, grav = orc.grav_accel(obody(orc, s), sem=orc.SEM_GPU)
+    nsi = s.n_SI
+    drag, dref = (a - a0)[nsi:], (ref - vec(grav))[nsi:]
+    bound = 1e-5 * np.linalg.norm(dref, axis=1) + 4e-16 * np.linalg.norm(a[nsi:], axis=1)
+    assert np.all(np.linalg.norm(drag - dref, axis=1) <= bound)
+    err = np.linalg.norm(a[nsi:] - ref[nsi:], axis=1) / np.linalg.norm(ref[nsi:], axis=1)
+    assert err.max() < 1e-9
+
+
 def run_oracle(orc, s, kind, dt, nsteps, adaptive, tol=0.0, gas=None, eftp=False):
     b = obody(orc, s)
     okind = {"euler": orc.EULER, "rk2": orc.RK2, "rk4": orc.RK4, "rkf78": orc.RKF78}[kind]
