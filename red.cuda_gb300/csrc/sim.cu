@@ -378,6 +378,15 @@ struct red_sim {
     DevSys* d_sys = nullptr;
     SysInfo* d_sinfo = nullptr;
     GravItem* d_items = nullptr;
+    // the work items of each system, items[item_begin[s], item_begin[s + 1]) (plans
+    // without clusters), and a device list of the items of the systems that a
+    // red_step retry still integrates
+    std::vector<size_t> item_begin;
+    std::vector<GravItem> sparse_items;
+    GravItem* d_sparse_items = nullptr;
+    size_t sparse_cap = 0;
+    const GravItem* items_override = nullptr;   // enqueue_try: launch these instead of the plan's items
+    int n_items_override = 0;
     size_t items_cap = 0;
     Segment* d_segs = nullptr;
     size_t segs_cap = 0;
@@ -445,6 +454,7 @@ struct red_sim {
     void enqueue_try(std::vector<int>* kinds = nullptr, std::vector<cudaEvent_t>* evs = nullptr);
     void capture();
     void launch_tries(uint32_t n);
+    bool launch_sparse_try(const std::vector<DevSys>& ds);
     void read_sys(std::vector<DevSys>& out);
     void write_sys(const std::vector<DevSys>& in);
     void prep_positions();
@@ -498,7 +508,7 @@ red_sim::~red_sim()
     for (int s = 0; s < kMaxStages; s++) cudaFree(Kv[s]);
     for (int k = 0; k < 2; k++) { cudaFree(pos_hi[k]); cudaFree(pos_lo[k]); }
     cudaFree(mass); cudaFree(radius); cudaFree(density); cudaFree(cd); cudaFree(id); cudaFree(btype);
-    cudaFree(partial); cudaFree(tile_cnt); cudaFree(d_sys); cudaFree(d_sinfo); cudaFree(d_items);
+    cudaFree(partial); cudaFree(tile_cnt); cudaFree(d_sys); cudaFree(d_sinfo); cudaFree(d_items); cudaFree(d_sparse_items);
     cudaFree(d_segs); cudaFree(d_pairs); cudaFree(d_events); cudaFree(d_nev); cudaFree(d_u);
     cudaFree(d_grid); cudaFree(d_head); cudaFree(d_next); cudaFree(d_cell); cudaFree(d_fsegs);
     cudaFree(d_xfer);
@@ -693,10 +703,12 @@ void red_sim::build_plan()
     long long short_ctas = 0;
     for (uint32_t s = 0; s < n_sys; s++) tiles_all += count_sink_tiles(sinfo[s], mode, lanes_cap, &short_ctas);
     const bool short_chunks = short_ctas <= 6 * 152;   // one wave at 6 CTAs per SM
+    item_begin.assign(n_sys + 1, 0);
     for (uint32_t s = 0; s < n_sys; s++) {
         const SysHost& h = sh[s];
         SysInfo& si = sinfo[s];
         (void)h;
+        item_begin[s] = items.size();
         star_mass[s] = si.n_star > 0 && h_id[si.off] >= 0 ? h_mass[si.off] : 0.0;
         plan_gravity_items(si, (int)s, mode, chunk_override, lanes_cap, tiles_all, short_chunks, &star_mass[s], items,
                            part, tiles);
@@ -737,6 +749,7 @@ void red_sim::build_plan()
     // one thread-block cluster and reduce through distributed shared memory:
     // no GPU-scope fence or global partial records on the critical path.
     // REDGB_CLUSTER=0 keeps the global reduction.
+    if (!item_begin.empty()) item_begin[n_sys] = items.size();
     use_cluster = false;
     const char* cenv = getenv("REDGB_CLUSTER");
     if ((mode == MODE_MIXED || mode == MODE_FP32) && chunk_override == 0 && !(cenv && cenv[0] == '0')) {
@@ -756,6 +769,7 @@ void red_sim::build_plan()
                 check_cluster_layout(cl);
                 items.swap(cl);
                 use_cluster = true;
+                item_begin.clear();   // the cluster layout interleaves the systems' items
             }
         }
     }
@@ -895,7 +909,8 @@ void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs
             P.head = d_head;
             P.head_n = (long long)table_size;
         }
-        launch_stage(P, (int)items.size(), mode, stream);
+        if (items_override) P.items = items_override;
+        launch_stage(P, items_override ? n_items_override : (int)items.size(), mode, stream);
         mark(0);
         n++;
     }
@@ -1036,6 +1051,50 @@ void red_sim::launch_tries(uint32_t n)
         CK(cudaGraphLaunch(graph, stream));
         launches += (uint64_t)launches_per_try;
     }
+}
+
+// One try over the work items of the systems a red_step still waits for (ds:
+// the system records after the previous try), launched directly instead of
+// the try's graph, whose stage launches would start a CTA for every item of
+// every system.  The same kernels and item records as the graph's, so the
+// results are the same bits.  Returns false (nothing launched) when the plan
+// interleaves the systems' items (cluster layout) or half the items or more
+// are still pending.
+bool red_sim::launch_sparse_try(const std::vector<DevSys>& ds)
+{
+    if (item_begin.size() != n_sys + 1 || !graph || ds.size() != n_sys) return false;
+    sparse_items.clear();
+    for (uint32_t s = 0; s < n_sys; s++) {
+        const DevSys& d = ds[s];
+        if (d.active && !d.halted && d.quota != 0)
+            sparse_items.insert(sparse_items.end(), items.begin() + item_begin[s], items.begin() + item_begin[s + 1]);
+    }
+    if (sparse_items.empty() || 2 * sparse_items.size() > items.size()) return false;
+    if (sparse_items.size() > sparse_cap) {
+        cudaFree(d_sparse_items);
+        d_sparse_items = nullptr;
+        sparse_cap = 0;
+        d_sparse_items = dalloc<GravItem>(sparse_items.size());
+        sparse_cap = sparse_items.size();
+    }
+    // a pageable source: the copy has read it when the call returns
+    CK(cudaMemcpyAsync(d_sparse_items, sparse_items.data(), sparse_items.size() * sizeof(GravItem),
+                       cudaMemcpyHostToDevice, stream));
+    const char* pe = getenv("REDGB_PDL");
+    set_pdl(!(pe && pe[0] == '0'));
+    items_override = d_sparse_items;
+    n_items_override = (int)sparse_items.size();
+    try {
+        enqueue_try();
+    } catch (...) {
+        items_override = nullptr;
+        set_pdl(false);
+        throw;
+    }
+    items_override = nullptr;
+    set_pdl(false);
+    launches += (uint64_t)launches_per_try;
+    return true;
 }
 
 void red_sim::read_sys(std::vector<DevSys>& out)
@@ -1441,7 +1500,8 @@ int red_step(red_sim* sim, double* dt_did)
         sim->launches++;
     }
     for (int guard = 0; guard < 100000; guard++) {
-        sim->launch_tries(1);
+        // retries of an ensemble launch only the items of the systems still pending
+        if (!(quota && guard > 0 && sim->launch_sparse_try(ds))) sim->launch_tries(1);
         sim->read_sys(ds);
         bool pending = false;
         for (const DevSys& d : ds) {
