@@ -392,9 +392,9 @@ __device__ __forceinline__ void gravity_f64(SmemStage& sm, const StageParams& P,
 // of each stage is on the critical path).  The per-variant instances run 7 CTAs
 // per SM (72 registers, 27 KB of shared memory each): their launches are many
 // waves of CTAs that each wait on a chain of memory round trips, and the seventh
-// CTA hides more of it (C4 ensemble stage -17 %, gas-drag disk -13 %, dense
-// -1.3 %; 8 CTAs at 64 registers spill and are slower).  The one-wave instance
-// keeps 80 registers.
+// CTA hides more of it (512-disk ensemble stage -17 %, 65536-body gas-drag
+// disk -13 %, all-pairs 16384-body disk -1.3 %; 8 CTAs at 64 registers spill
+// and are slower).  The one-wave instance keeps 80 registers.
 template <int MODE, bool EXACT, bool CL, int VT>
 __global__ void __launch_bounds__(kTile, VT >= 0 ? 7 : 6) k_stage(const StageParams P, const int Vrt)
 {

@@ -1,14 +1,14 @@
 """The bench's workloads at their full sizes, checked through size-independent
 properties (the oracle would take minutes at these sizes).
 
-* C2 (N = 16384, MIXED, adaptive RKF7(8) at tol 1e-10; collisions off, since a
+* the 16384-body disk (MIXED, adaptive RKF7(8) at tol 1e-10; collisions off, since a
   perfect merge changes E by design): energy over the interacting pairs
   conserved to |dE/E| < 1e-9 and the angular momentum to 1e-10 over 300 tries,
   the metric's accuracy bar.
-* C4 (512 disks, 1.08 M bodies): the same bar for every disk after 30 tries,
+* the 512-disk ensemble (1.08 M bodies): the same bar for every disk after 30 tries,
   and the ensemble's counters consistent (tried = passed + failed).
-* dense C2 (every pair interacts): the same bar after 8 tries.
-* C1 (N = 2053, RK4 fixed step): MIXED against FP64 after 100 steps, 1e-10
+* the same disk with every pair interacting: the same bar after 8 tries.
+* the 2053-body disk (RK4 fixed step): MIXED against FP64 after 100 steps, 1e-10
   relative in position (the precision modes agree at full size).
 """
 import numpy as np
