@@ -98,15 +98,14 @@ __global__ void k_control(const ControlParams P)
 // Spatial-hash broad phase for the small bodies.  Cell coordinates are
 // clamped so that far-away bodies share border cells (tested exactly, never
 // missed).
-__device__ __forceinline__ int4 cell_of(double x, double y, double z, double inv_h)
+__device__ __forceinline__ int cell_coord(double x, double inv_h)
 {
     const double lim = 1.0e9;
-    int4 c;
-    c.x = (int)floor(fmin(fmax(x * inv_h, -lim), lim));
-    c.y = (int)floor(fmin(fmax(y * inv_h, -lim), lim));
-    c.z = (int)floor(fmin(fmax(z * inv_h, -lim), lim));
-    c.w = 0;
-    return c;
+    return (int)floor(fmin(fmax(x * inv_h, -lim), lim));
+}
+__device__ __forceinline__ int4 cell_of(double x, double y, double z, double inv_h)
+{
+    return make_int4(cell_coord(x, inv_h), cell_coord(y, inv_h), cell_coord(z, inv_h), 0);
 }
 
 __device__ __forceinline__ int bucket_of(int cx, int cy, int cz, int mask)
@@ -170,18 +169,26 @@ __global__ void __launch_bounds__(4 * kFinishBodies) k_finish(const FinishParams
         }
         P.y_r[x] = r;
         P.y_v[x] = v;
-        if (!(isfinite(r) && isfinite(v))) S->status = 5;   // RED_ERR_NONFINITE
+        // finiteness from the exponent bits (integer pipe, not the FP64 pipe)
+        const long long br = __double_as_longlong(r), bv = __double_as_longlong(v);
+        if (((br >> 52) & 0x7ff) == 0x7ff || ((bv >> 52) & 0x7ff) == 0x7ff) S->status = 5;   // RED_ERR_NONFINITE
     } else {
         r = P.y_r[x];
     }
     write_pos_c(P.pos_hi0, P.pos_lo0, i, c, r);
     if (P.head && acc) {
+        // lanes 0..2 form the cell coordinate of their own component (the FP64
+        // pipe runs a warp instruction at the same cost for 8 lanes as for 32,
+        // so the three components go side by side), lane 3 inserts the body
+        const GridInfo g = P.grid[sg.sys];
         const int l0 = (int)(threadIdx.x & 31u) & ~3;
         const unsigned gm = 0xFu << l0;   // the body's four lanes
-        const double rx = __shfl_sync(gm, r, l0), ry = __shfl_sync(gm, r, l0 + 1), rz = __shfl_sync(gm, r, l0 + 2);
-        const GridInfo g = P.grid[sg.sys];
-        if (c == 3 && g.enabled && i >= P.sinfo[sg.sys].off + P.sinfo[sg.sys].n_SI)
-            grid_insert_one(g, P.cell, P.next, P.head, i, rx, ry, rz);
+        const int cc = (g.enabled && c < 3) ? cell_coord(r, g.inv_h) : 0;
+        const int4 cl = make_int4(__shfl_sync(gm, cc, l0), __shfl_sync(gm, cc, l0 + 1), __shfl_sync(gm, cc, l0 + 2), 0);
+        if (c == 3 && g.enabled && i >= P.sinfo[sg.sys].off + P.sinfo[sg.sys].n_SI) {
+            P.cell[i] = cl;
+            P.next[i] = atomicExch(&P.head[g.toff + bucket_of(cl.x, cl.y, cl.z, g.mask)], i);
+        }
     }
 }
 
