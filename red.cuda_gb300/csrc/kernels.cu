@@ -123,71 +123,77 @@ __device__ __forceinline__ void grid_insert_one(const GridInfo& g, int4* cell, i
     next[i] = atomicExch(&head[g.toff + bucket_of(c.x, c.y, c.z, g.mask)], i);
 }
 
-// y_{n+1} of the accepted systems and the positions of the next stage 0.  Four
-// threads per body: lanes 0..2 the x, y, z components, lane 3 the mass / radius
-// words of the FP32 copies.  Segments of kFinishBodies bodies.
+// y_{n+1} of the accepted systems and the positions of the next stage 0.  One
+// thread per component: element e of a segment of kFinishBodies bodies is
+// component e % 3 of body e / 3, contiguous in memory, so every FP64 warp
+// instruction runs on full warps (the FP64 pipe charges a warp instruction the
+// same for any number of active lanes).  The threads then form the hash-cell
+// coordinate of their component, and one thread per small body inserts it
+// into the collision check's spatial hash.
 template <bool EXACT>
-__global__ void __launch_bounds__(4 * kFinishBodies) k_finish(const FinishParams P)
+__global__ void __launch_bounds__(3 * kFinishBodies) k_finish(const FinishParams P)
 {
     pdl_wait();
     pdl_trigger();
+    __shared__ int cellc[3 * kFinishBodies];
     const Segment sg = P.segs[blockIdx.x];
     DevSys* S = P.sys + sg.sys;
     if (S->halted) return;
-    const int i = sg.b0 + threadIdx.x / 4;
-    const int c = threadIdx.x % 4;
     const bool acc = S->accepted;
     if (!acc && !runnable(*S)) return;   // uniform over the CTA
-    if (i >= sg.b1) return;              // uniform over the body's four lanes
-    // lane 3 holds no component (the .w words, mass and radius, are set by
-    // k_prep); it inserts the body into the collision check's spatial hash
-    const int x = 3 * i + min(c, 2);
+    const int e = threadIdx.x;
+    const int nb = sg.b1 - sg.b0;
+    const bool live = e < 3 * nb;
+    const int i = sg.b0 + e / 3;
+    const int c = e % 3;
+    const int x = 3 * sg.b0 + e;
     double r = 0.0;
-    if (c == 3) {
-    } else if (acc) {
-        const double dt = S->dt_did;
-        double v;
-        if (P.scheme == SCHEME_RKF78) {
-            r = rk8_ynp1<EXACT>(P.y_r[x], dt, P.Kr, x);
-            v = rk8_ynp1<EXACT>(P.y_v[x], dt, P.Kv, x);
-        } else if (P.scheme == SCHEME_EULER) {
-            // euler::calc_y_np1 -> sum_vector, int_euler.cu:19-31, 54-71: y + dt f0
-            r = madd<EXACT>(P.y_r[x], dt, P.Kr[0][x]);
-            v = madd<EXACT>(P.y_v[x], dt, P.Kv[0][x]);
-        } else if (P.scheme == SCHEME_RK2) {
-            // rungekutta2::calc_y_np1, int_rungekutta2.cu:66-83: y + (b_1 dt) f2
-            const double bf = mul<EXACT>(c_tb.b2[1], dt);
-            r = madd<EXACT>(P.y_r[x], bf, P.Kr[1][x]);
-            v = madd<EXACT>(P.y_v[x], bf, P.Kv[1][x]);
-        } else if (P.commit_from_stage4) {
-            r = P.t_r0[x];
-            v = P.Kr[4][x];
+    if (live) {
+        if (acc) {
+            const double dt = S->dt_did;
+            double v;
+            if (P.scheme == SCHEME_RKF78) {
+                r = rk8_ynp1<EXACT>(P.y_r[x], dt, P.Kr, x);
+                v = rk8_ynp1<EXACT>(P.y_v[x], dt, P.Kv, x);
+            } else if (P.scheme == SCHEME_EULER) {
+                // euler::calc_y_np1 -> sum_vector, int_euler.cu:19-31, 54-71: y + dt f0
+                r = madd<EXACT>(P.y_r[x], dt, P.Kr[0][x]);
+                v = madd<EXACT>(P.y_v[x], dt, P.Kv[0][x]);
+            } else if (P.scheme == SCHEME_RK2) {
+                // rungekutta2::calc_y_np1, int_rungekutta2.cu:66-83: y + (b_1 dt) f2
+                const double bf = mul<EXACT>(c_tb.b2[1], dt);
+                r = madd<EXACT>(P.y_r[x], bf, P.Kr[1][x]);
+                v = madd<EXACT>(P.y_v[x], bf, P.Kv[1][x]);
+            } else if (P.commit_from_stage4) {
+                r = P.t_r0[x];
+                v = P.Kr[4][x];
+            } else {
+                const double b0 = mul<EXACT>(c_tb.b4[0], dt), b1 = mul<EXACT>(c_tb.b4[1], dt);
+                r = rk4_ynp1<EXACT>(P.y_r[x], b0, b1, P.Kr[0][x], P.Kr[1][x], P.Kr[2][x], P.Kr[3][x]);
+                v = rk4_ynp1<EXACT>(P.y_v[x], b0, b1, P.Kv[0][x], P.Kv[1][x], P.Kv[2][x], P.Kv[3][x]);
+            }
+            P.y_r[x] = r;
+            P.y_v[x] = v;
+            // finiteness from the exponent bits (integer pipe, not the FP64 pipe)
+            const long long br = __double_as_longlong(r), bv = __double_as_longlong(v);
+            if (((br >> 52) & 0x7ff) == 0x7ff || ((bv >> 52) & 0x7ff) == 0x7ff) S->status = 5;   // RED_ERR_NONFINITE
         } else {
-            const double b0 = mul<EXACT>(c_tb.b4[0], dt), b1 = mul<EXACT>(c_tb.b4[1], dt);
-            r = rk4_ynp1<EXACT>(P.y_r[x], b0, b1, P.Kr[0][x], P.Kr[1][x], P.Kr[2][x], P.Kr[3][x]);
-            v = rk4_ynp1<EXACT>(P.y_v[x], b0, b1, P.Kv[0][x], P.Kv[1][x], P.Kv[2][x], P.Kv[3][x]);
+            r = P.y_r[x];
         }
-        P.y_r[x] = r;
-        P.y_v[x] = v;
-        // finiteness from the exponent bits (integer pipe, not the FP64 pipe)
-        const long long br = __double_as_longlong(r), bv = __double_as_longlong(v);
-        if (((br >> 52) & 0x7ff) == 0x7ff || ((bv >> 52) & 0x7ff) == 0x7ff) S->status = 5;   // RED_ERR_NONFINITE
-    } else {
-        r = P.y_r[x];
+        // x, y, z of the FP32 copies; k_prep holds the .w words (mass, radius)
+        write_pos_c(P.pos_hi0, P.pos_lo0, i, c, r);
     }
-    write_pos_c(P.pos_hi0, P.pos_lo0, i, c, r);
-    if (P.head && acc) {
-        // lanes 0..2 form the cell coordinate of their own component (the FP64
-        // pipe runs a warp instruction at the same cost for 8 lanes as for 32,
-        // so the three components go side by side), lane 3 inserts the body
+    if (P.head && acc) {   // uniform over the CTA
         const GridInfo g = P.grid[sg.sys];
-        const int l0 = (int)(threadIdx.x & 31u) & ~3;
-        const unsigned gm = 0xFu << l0;   // the body's four lanes
-        const int cc = (g.enabled && c < 3) ? cell_coord(r, g.inv_h) : 0;
-        const int4 cl = make_int4(__shfl_sync(gm, cc, l0), __shfl_sync(gm, cc, l0 + 1), __shfl_sync(gm, cc, l0 + 2), 0);
-        if (c == 3 && g.enabled && i >= P.sinfo[sg.sys].off + P.sinfo[sg.sys].n_SI) {
-            P.cell[i] = cl;
-            P.next[i] = atomicExch(&P.head[g.toff + bucket_of(cl.x, cl.y, cl.z, g.mask)], i);
+        if (!g.enabled) return;
+        if (live) cellc[e] = cell_coord(r, g.inv_h);
+        __syncthreads();
+        const int small0 = P.sinfo[sg.sys].off + P.sinfo[sg.sys].n_SI;
+        if (e < nb && sg.b0 + e >= small0) {
+            const int b = sg.b0 + e;
+            const int4 cl = make_int4(cellc[3 * e], cellc[3 * e + 1], cellc[3 * e + 2], 0);
+            P.cell[b] = cl;
+            P.next[b] = atomicExch(&P.head[g.toff + bucket_of(cl.x, cl.y, cl.z, g.mask)], b);
         }
     }
 }
@@ -572,8 +578,8 @@ void launch_control(const ControlParams& P, cudaStream_t s)
 void launch_finish(const FinishParams& P, int n_segs, cudaStream_t s)
 {
     if (n_segs <= 0) return;
-    if (P.stage_exact) launch_k(k_finish<true>, (unsigned)n_segs, 4u * kFinishBodies, s, P);
-    else launch_k(k_finish<false>, (unsigned)n_segs, 4u * kFinishBodies, s, P);
+    if (P.stage_exact) launch_k(k_finish<true>, (unsigned)n_segs, 3u * kFinishBodies, s, P);
+    else launch_k(k_finish<false>, (unsigned)n_segs, 3u * kFinishBodies, s, P);
 }
 
 // The explicit collision check (red_check_for_collision) on the current state.

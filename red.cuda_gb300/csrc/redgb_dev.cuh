@@ -19,7 +19,7 @@ namespace redgb {
 
 constexpr int kTile = 128;          // sinks per CTA and sources per shared-memory tile
 constexpr int kSegment = 256;       // bodies per CTA in the per-body kernels
-constexpr int kFinishBodies = 64;   // bodies per CTA of k_finish (four threads each)
+constexpr int kFinishBodies = 64;   // bodies per CTA of k_finish (one thread per component)
 constexpr int kClusterChunks = 16;  // source chunks of a tile in a cluster launch (one cluster)
 constexpr int kMaxStages = 13;
 
