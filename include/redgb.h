@@ -255,9 +255,14 @@ int red_populate_disks(const red_disk_spec_t* specs, uint32_t n_systems, int32_t
  * stream.  Temporaries live in a fixed 4 MiB __device__ array inside the
  * library, held by every GPU that loads it until exit; calls share it, so
  * calls that overlap on the GPU race and must be ordered by the caller.  The
- * first call on a device looks the array up and loads constant tables: make
- * it before any stream capture.  Systems above RED_NOALLOC_MAX_BODIES bodies
- * are rejected with RED_ERR_ARG. */
+ * first call on a device does a one-time set-up (it looks up the device
+ * address of the array): make that first call before any stream capture.
+ * The call writes no constant memory, so simulations created earlier keep
+ * their integrator coefficients.  Every system of up to
+ * RED_NOALLOC_MAX_BODIES bodies fits, whatever its body classes (a plan that
+ * would need more partial-sum records than the array holds falls back to
+ * unchunked source lists); larger systems are rejected with RED_ERR_ARG.
+ * The caller's current device is the same after the call as before it. */
 #define RED_NOALLOC_MAX_BODIES 32768
 typedef struct {
     uint32_t playing[RED_BODY_N];  /* bodies per type; bodies sorted by type */

@@ -16,9 +16,16 @@
 // race on it -- callers must order them.
 //
 // The first call on a device looks up the device address of the array with
-// cudaGetSymbolAddress (with that device current) and loads the integrator
-// tableau into constant memory; make that first call before any stream
-// capture.
+// cudaGetSymbolAddress (with that device current); make that first call
+// before any stream capture.  The entry point writes no constant memory: a
+// standalone evaluation reads no integrator coefficients, and the tableau
+// that live simulations loaded stays as it is.
+//
+// Every system of at most RED_NOALLOC_MAX_BODIES bodies fits: when the
+// allocating path's launch plan (sources split into chunks whose partial sums
+// need scratch records) does not fit the array, the plan falls back to one
+// CTA per sink tile over the whole source list, which needs no partial
+// records and at most n / 16 + 3 work items.
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -84,6 +91,7 @@ extern "C" int red_calc_accel_noalloc(const red_accel_args_t* a)
     if (a->precision < 0 || a->precision > 3) return fail(RED_ERR_ARG, "bad precision");
     if (a->device < 0 || a->device >= kMaxDevices) return fail(RED_ERR_ARG, "bad device");
     const size_t pos_bytes = (size_t)n * sizeof(float4);
+    const size_t off_part = ((kOffPos + 2 * pos_bytes + 255) / 256) * 256;
 
     // the launch plan, on the host
     SysInfo si;
@@ -97,13 +105,30 @@ extern "C" int red_calc_accel_noalloc(const red_accel_args_t* a)
     std::vector<GravItem> items;
     size_t part = 0;
     int tiles = 0;
+    auto fits = [&]() {
+        return items.size() <= kMaxItems && (size_t)tiles <= kMaxTiles &&
+               off_part + part * 3 * sizeof(double) <= kScratchBytes;
+    };
     long long short_ctas = 0;
     const int tiles_all = count_sink_tiles(si, a->precision, 32, &short_ctas);
     plan_gravity_items(si, 0, a->precision, 0, 32, tiles_all, short_ctas <= 6 * 152, nullptr, items, part, tiles);
-    const size_t off_part = ((kOffPos + 2 * pos_bytes + 255) / 256) * 256;
-    if (items.size() > kMaxItems || (size_t)tiles > kMaxTiles || off_part + part * 3 * sizeof(double) > kScratchBytes)
-        return fail(RED_ERR_ARG, "red_calc_accel_noalloc: the launch plan does not fit the scratch array");
+    if (!fits()) {
+        // unchunked: one chunk spans all n bodies, and 8 lanes per sink group
+        // give tiles of >= 16 sinks, so no partial records and few items
+        items.clear();
+        part = 0;
+        tiles = 0;
+        plan_gravity_items(si, 0, a->precision, (int)n, 8, tiles_all, false, nullptr, items, part, tiles);
+    }
+    if (!fits()) return fail(RED_ERR_ARG, "red_calc_accel_noalloc: the launch plan does not fit the scratch array");
 
+    // the caller's current device is restored on every return path
+    int prev_device = -1;
+    if (cudaGetDevice(&prev_device) != cudaSuccess) return fail(RED_ERR_CUDA, "cudaGetDevice failed");
+    struct DeviceGuard {
+        int prev;
+        ~DeviceGuard() { cudaSetDevice(prev); }
+    } guard{prev_device};
     if (cudaSetDevice(a->device) != cudaSuccess) return fail(RED_ERR_CUDA, "cudaSetDevice failed");
     void* base = nullptr;
     {
@@ -126,9 +151,6 @@ extern "C" int red_calc_accel_noalloc(const red_accel_args_t* a)
     float4* d_lo = (float4*)(b + kOffPos + pos_bytes);
     double* d_part = (double*)(b + off_part);
 
-    Tableau tb;
-    memset(&tb, 0, sizeof(tb));
-    set_tableau(tb, st);   // stage times are not used by a standalone evaluation
     if (cudaMemcpyAsync(d_items, items.data(), items.size() * sizeof(GravItem), cudaMemcpyHostToDevice, st) !=
             cudaSuccess ||
         cudaMemsetAsync(d_tiles, 0, kMaxTiles * sizeof(unsigned), st) != cudaSuccess ||

@@ -12,7 +12,13 @@ systems, so that nothing left in the shared array by the first call leaks
 into the second.  Tolerance: the same launch plan and summation order (the
 allocating side keeps the global chunk reduction, REDGB_CLUSTER=0, as the
 allocation-free entry point does), so the results agree to 1e-12 relative
-(they are expected to be identical).
+(they are expected to be identical).  At the largest accepted size, a dense
+system whose chunked plan would overflow the scratch array, the entry point
+sums each sink's sources in one CTA instead of in chunks, which reorders the
+double-single accumulation: 1e-10 relative there.
+
+A live simulation must not notice the entry point: a Sim stepped across a
+call follows the same trajectory, bit for bit, as one that never saw it.
 """
 import ctypes as C
 
@@ -68,7 +74,7 @@ def reference(rg, s, precision, t=0.0, gas=None):
             os.environ["REDGB_CLUSTER"] = old
 
 
-@pytest.mark.parametrize("precision", ["mixed", "fp64_exact"])
+@pytest.mark.parametrize("precision", ["mixed", "fp32", "fp64", "fp64_exact"])
 def test_noalloc_matches_allocating_entry_point_twice(rg, precision):
     torch = pytest.importorskip("torch")
     from redgb.lib import calc_accel_noalloc
@@ -107,3 +113,51 @@ def test_noalloc_rejects_oversized_systems(rg):
     with pytest.raises(RedError) as e:
         calc_accel_noalloc(a)
     assert e.value.code == 1 and "RED_NOALLOC_MAX_BODIES" in str(e.value)
+
+
+def test_noalloc_leaves_live_simulations_alone(rg):
+    """Steps of a Sim created before a call match those of a Sim that never saw one."""
+    torch = pytest.importorskip("torch")
+    from redgb.lib import calc_accel_noalloc
+    s = rg.ic.config2(seed=43, n_pp=6, n_pl=1500)
+    other = rg.ic.config1(seed=44, n_pl=700)
+    runs = []
+    for with_call in (False, True):
+        with rg.Sim(s, dt=0.5 * rg.ic.K, precision="mixed") as sim:
+            for k in range(6):
+                if with_call and k in (1, 4):
+                    a, keep = device_args(rg, torch, other, "fp64")
+                    calc_accel_noalloc(a)
+                    torch.cuda.synchronize()
+                sim.step()
+            st = sim.get_state(0)
+            runs.append((vec(st.r), vec(st.v), sim.info(0).t))
+    assert runs[0][2] == runs[1][2]
+    assert np.array_equal(runs[0][0], runs[1][0]) and np.array_equal(runs[0][1], runs[1][1])
+
+
+def test_noalloc_largest_dense_system(rg):
+    """RED_NOALLOC_MAX_BODIES bodies, every pair interacting (all protoplanets)."""
+    torch = pytest.importorskip("torch")
+    from redgb.lib import NOALLOC_MAX_BODIES, calc_accel_noalloc
+    s = rg.ic.config2(seed=45, n_pp=16, n_pl=NOALLOC_MAX_BODIES - 17).relabel_all_SI()
+    assert s.n == NOALLOC_MAX_BODIES
+    ref = reference(rg, s, "mixed")
+    for _ in range(2):
+        a, keep = device_args(rg, torch, s, "mixed")
+        calc_accel_noalloc(a)
+        torch.cuda.synchronize()
+        got = keep["accel"].cpu().numpy().reshape(-1, 3)
+        err = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+        assert err.max() <= 1e-10, err.max()
+
+
+def test_noalloc_restores_current_device(rg):
+    torch = pytest.importorskip("torch")
+    from redgb.lib import calc_accel_noalloc
+    s = rg.ic.config1(seed=46, n_pl=300)
+    before = torch.cuda.current_device()
+    a, keep = device_args(rg, torch, s, "mixed")
+    calc_accel_noalloc(a)
+    torch.cuda.synchronize()
+    assert torch.cuda.current_device() == before
