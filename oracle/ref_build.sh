@@ -1,7 +1,11 @@
 #!/usr/bin/env bash
 # Builds oracle/_ref/ref_harness from the reference's own, unmodified sources
-# (suliaron/red.cuda mounted read-only at /root/reference).  Test
-# infrastructure: the binary only produces golden vectors for tests/golden/.
+# (suliaron/red.cuda mounted read-only at /root/reference, or the directory
+# named by RED_REFERENCE).  Test infrastructure: the binary produces golden
+# vectors for tests/golden/ on the CPU and, built on a machine with a GPU from
+# the staged copy (oracle/ref_stage.sh; RED_REFERENCE=baseline/_ref/red.cuda,
+# RED_REF_OUT=oracle/_ref/box), runs red's own GPU path for the parity pins
+# and the plain-FP64 baseline.
 #
 # Two build-time shims, no source edits:
 #   -DclockRate=maxThreadsPerBlock  cudaDeviceProp::clockRate was removed in
@@ -14,7 +18,7 @@
 set -euo pipefail
 REF=${RED_REFERENCE:-/root/reference}
 HERE="$(cd "$(dirname "$0")" && pwd)"
-OUT="$HERE/_ref"
+OUT="${RED_REF_OUT:-$HERE/_ref}"
 mkdir -p "$OUT/obj"
 [ -d "$REF/src/red.cuda" ] || { echo "reference not found at $REF" >&2; exit 3; }
 

@@ -18,6 +18,16 @@
 //   ej= hc=                       (mode=ejhc)
 //   gasdir= gas= t=               (mode=accel: adds drag on NSI bodies)
 //   odir=                         (mode=dump: red's own print_data/print_data_info)
+//   dev=cpu|gpu                   gpu: red's own GPU path (pp_disk on COMPUTING_DEVICE_GPU,
+//                                 copy_to_device, the n_tpb search of run_simulation,
+//                                 main.cu:449-463); accel writes red's gravity + drag as one
+//                                 array, run times the step loop, coll writes the raw events
+//   tpb=                          (dev=gpu) threads per block instead of red's search
+//   tout=                         (dev=gpu, mode=run) file for the step loop's wall time
+//
+// With dev=gpu the binary must be built on the machine that has the GPU
+// (oracle/ref_build.sh, from a staged copy of the unmodified sources).
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -86,18 +96,41 @@ int main(int argc, char** argv)
         thr[THRESHOLD_RADII_ENHANCE_FACTOR] = atof(arg("factor", "0").c_str());
         string gas = arg("gas");
         gas_disk_model_t gdm = gas.empty() ? GAS_DISK_MODEL_NONE : GAS_DISK_MODEL_ANALYTIC;
-        pp_disk* ppd = new pp_disk(path_data, path_info, gdm, 0, COMPUTING_DEVICE_CPU, thr);
+        const bool gpu = arg("dev", "cpu") == "gpu";
+        const computing_device_t cdev = gpu ? COMPUTING_DEVICE_GPU : COMPUTING_DEVICE_CPU;
+        pp_disk* ppd = new pp_disk(path_data, path_info, gdm, 0, cdev, thr);
         if (!gas.empty()) {
             string gdir = arg("gasdir");
             ppd->a_gd = new analytic_gas_disk(gdir, gas, false);
             ppd->a_gd->calc(ppd->get_mass_of_star());
+        }
+        if (gpu) {
+            // options::create_pp_disk (options.cpp:239-242), then run_simulation's
+            // thread-per-block search (main.cu:449-463)
+            ppd->copy_to_device();
+            const int tpb = atoi(arg("tpb", "0").c_str());
+            ppd->set_n_tpb(tpb > 0 ? (uint32_t)tpb : ppd->benchmark(false));
         }
         string mode = arg("mode", "run");
         FILE* f = fopen(arg("out").c_str(), "wb");
         if (!f && mode != "dump") throw string("cannot open out");
         const uint32_t n = ppd->n_bodies->get_n_total_playing();
 
-        if (mode == "accel") {
+        if (mode == "accel" && gpu) {
+            // red's calc_dydx(1, ...) on the device: the SI, NSI and NI launches of
+            // calc_grav_accel_naive, then calc_drag_accel_NSI (pp_disk.cu:1450-1502, 1014-1060)
+            vector<var4_t> a(n);
+            var_t t = atof(arg("t", "0").c_str());
+            var4_t* d_dy = 0;
+            if (cudaMalloc((void**)&d_dy, n * sizeof(var4_t)) != cudaSuccess) throw string("cudaMalloc");
+            cudaMemset(d_dy, 0, n * sizeof(var4_t));
+            ppd->calc_dydx(1, 0, t, ppd->sim_data->y[0], ppd->sim_data->y[1], d_dy);
+            if (cudaMemcpy(&a[0], d_dy, n * sizeof(var4_t), cudaMemcpyDeviceToHost) != cudaSuccess)
+                throw string("cudaMemcpy");
+            int grav_ok = 1;
+            put(f, &grav_ok, 4);
+            put(f, &a[0], n * sizeof(var4_t));
+        } else if (mode == "accel") {
             // gravity through red's CPU path (SI symmetric + NI), then drag on the NSI bodies
             vector<var4_t> a(n), d(n);
             var_t t = atof(arg("t", "0").c_str());
@@ -123,12 +156,17 @@ int main(int argc, char** argv)
             var_t tol = atof(arg("tol", "1e-10").c_str());
             int nsteps = atoi(arg("nsteps", "1").c_str());
             integrator* ig = 0;
-            if (kind == 1) ig = new euler(ppd, ppd->dt, COMPUTING_DEVICE_CPU);
-            else if (kind == 2) ig = new rungekutta2(ppd, ppd->dt, COMPUTING_DEVICE_CPU);
-            else if (kind == 4) ig = new rungekutta4(ppd, ppd->dt, adaptive, tol, COMPUTING_DEVICE_CPU);
-            else ig = new rungekutta8(ppd, ppd->dt, adaptive, tol, COMPUTING_DEVICE_CPU);
+            if (kind == 1) ig = new euler(ppd, ppd->dt, cdev);
+            else if (kind == 2) ig = new rungekutta2(ppd, ppd->dt, cdev);
+            else if (kind == 4) ig = new rungekutta4(ppd, ppd->dt, adaptive, tol, cdev);
+            else ig = new rungekutta8(ppd, ppd->dt, adaptive, tol, cdev);
             ig->error_check_for_tp = atoi(arg("eftp", "0").c_str()) != 0;
             put(f, &nsteps, 4);
+            // the step loop's wall time (dev=gpu: every launch of red's path ends in a
+            // device synchronisation, red_macro.h:33, 62-90)
+            if (gpu) cudaDeviceSynchronize();
+            const auto t_start = std::chrono::steady_clock::now();
+            double t_steps = 0.0;
             for (int s = 0; s < nsteps; s++) {
                 ttt_t dt = ig->step();
                 ttt_t dtn = ig->get_dt_next();
@@ -138,10 +176,28 @@ int main(int argc, char** argv)
                 put(f, &dtn, 8);
                 put(f, c, 24);
             }
+            if (gpu) cudaDeviceSynchronize();
+            t_steps = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+            if (!arg("tout").empty()) {
+                FILE* ft = fopen(arg("tout").c_str(), "w");
+                if (!ft) throw string("cannot open tout");
+                fprintf(ft, "%.9f %u\n", t_steps, (unsigned)ppd->n_tpb);
+                fclose(ft);
+            }
+            if (gpu) ppd->copy_to_host();
             put_state(f, ppd);
             pp_disk_t::integral_t I;
             ppd->calc_integral(false, I);
             put(f, &I, sizeof(I));
+        } else if (mode == "coll" && gpu) {
+            // red's GPU check (pp_disk.cu:320-371, 1203-1218): the caller has counted the
+            // pairs beforehand, so the unchecked event buffer of n records
+            // (pp_disk.cu:1623-1628) holds them
+            ppd->t = atof(arg("t", "0").c_str());
+            ppd->check_for_collision();
+            ppd->copy_event_data_to_host();
+            vector<pp_disk_t::event_data_t> raw(ppd->events, ppd->events + ppd->event_counter);
+            put_events(f, raw);
         } else if (mode == "coll") {
             ppd->t = atof(arg("t", "0").c_str());
             ppd->check_for_collision();

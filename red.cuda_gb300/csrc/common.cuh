@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <utility>
 
+#include "crmath.cuh"
 #include "redgb_dev.cuh"
 
 namespace redgb {
@@ -220,7 +221,27 @@ template <bool EXACT> __device__ __forceinline__ double madd(double a, double b,
 // ---------------------------------------------------------------------------
 // analytic gas disk, pp_disk.cu:59-155 and 485-521
 // ---------------------------------------------------------------------------
-static __device__ double gas_reduction_factor(const GasDev& g, double t)
+// In the red-exact mode (EXACT) every operation is one rounding in red's
+// order (no contraction into FMA) and exp / pow return the nearest double
+// (crmath.cuh), as the C library's functions in red's CPU twin do.
+template <bool EXACT> __device__ __forceinline__ double dexp(double x)
+{
+    return EXACT ? crmath::cr_exp(x) : exp(x);
+}
+template <bool EXACT> __device__ __forceinline__ double dpow(double x, double y)
+{
+    return EXACT ? crmath::cr_pow(x, y) : pow(x, y);
+}
+template <bool EXACT> __device__ __forceinline__ double ddiv(double a, double b)
+{
+    return EXACT ? __ddiv_rn(a, b) : a / b;
+}
+template <bool EXACT> __device__ __forceinline__ double dsqrt(double a)
+{
+    return EXACT ? __dsqrt_rn(a) : sqrt(a);
+}
+
+template <bool EXACT> static __device__ double gas_reduction_factor(const GasDev& g, double t)
 {
     switch (g.gas_decrease) {
     case 0: return 1.0;
@@ -228,7 +249,7 @@ static __device__ double gas_reduction_factor(const GasDev& g, double t)
         if (t <= g.t0) return 1.0;
         else if (g.t0 < t && t <= g.t1 && g.t0 != g.t1) return 1.0 - (t - g.t0) / (g.t1 - g.t0);
         else return 0.0;
-    case 2: return exp(-(t - g.t0) / g.e_folding_time);
+    case 2: return dexp<EXACT>(ddiv<EXACT>(-sub<EXACT>(t, g.t0), g.e_folding_time));
     default: return 1.0;
     }
 }
@@ -236,13 +257,14 @@ static __device__ double gas_reduction_factor(const GasDev& g, double t)
 // Drag factor f and gas velocity (gx, gy, 0) at (r, v): the acceleration is
 // f (v_gas - v) (calc_drag_accel_NSI, pp_disk.cu:485-521).  red's FP64
 // arithmetic, for the FP64 modes.
-static __device__ void drag_factor(const GasDev& g, double decr, double m_star, double rx, double ry, double rz, double vx,
-                            double vy, double vz, double cd, double radius, double density, double& f, double& gx,
-                            double& gy)
+template <bool EXACT>
+static __device__ void drag_factor(const GasDev& g, double decr, double m_star, double rx, double ry, double rz,
+                                   double vx, double vy, double vz, double cd, double radius, double density,
+                                   double& f, double& gx, double& gy)
 {
     // gas velocity: circular velocity scaled by sqrt(1 - 2 eta r^p) (pp_disk.cu:107-155)
-    const double r = sqrt(rx * rx + ry * ry);
-    const double vc = sqrt(m_star / r);
+    const double r = dsqrt<EXACT>(add<EXACT>(mul<EXACT>(rx, rx), mul<EXACT>(ry, ry)));
+    const double vc = dsqrt<EXACT>(ddiv<EXACT>(m_star, r));
     gx = 0.0;
     gy = 0.0;
     if (rx == 0.0 && ry == 0.0) {
@@ -251,30 +273,37 @@ static __device__ void drag_factor(const GasDev& g, double decr, double m_star, 
     } else if (rx == 0.0) {
         gx = ry > 0.0 ? -vc : vc;
     } else if (rx >= ry) {
-        const double p = ry / rx;
-        gy = rx >= 0 ? vc / sqrt(1.0 + p * p) : -vc / sqrt(1.0 + p * p);
-        gx = -gy * p;
+        const double p = ddiv<EXACT>(ry, rx);
+        const double q = dsqrt<EXACT>(add<EXACT>(1.0, mul<EXACT>(p, p)));
+        gy = rx >= 0 ? ddiv<EXACT>(vc, q) : ddiv<EXACT>(-vc, q);
+        gx = mul<EXACT>(-gy, p);
     } else {
-        const double p = rx / ry;
-        gx = ry >= 0 ? -vc / sqrt(1.0 + p * p) : vc / sqrt(1.0 + p * p);
-        gy = -gx * p;
+        const double p = ddiv<EXACT>(rx, ry);
+        const double q = dsqrt<EXACT>(add<EXACT>(1.0, mul<EXACT>(p, p)));
+        gx = ry >= 0 ? ddiv<EXACT>(-vc, q) : ddiv<EXACT>(vc, q);
+        gy = mul<EXACT>(-gx, p);
     }
-    const double fv = sqrt(1.0 - 2.0 * g.eta[0] * pow(r, g.eta[1]));
-    gx *= fv;
-    gy *= fv;
+    const double fv =
+        dsqrt<EXACT>(sub<EXACT>(1.0, mul<EXACT>(mul<EXACT>(2.0, g.eta[0]), dpow<EXACT>(r, g.eta[1]))));
+    gx = mul<EXACT>(gx, fv);
+    gy = mul<EXACT>(gy, fv);
     // gas density (pp_disk.cu:86-105)
-    const double h = g.sch[0] * pow(r, g.sch[1]);
-    const double arg = (rz / h) * (rz / h);
+    const double h = mul<EXACT>(g.sch[0], dpow<EXACT>(r, g.sch[1]));
+    const double zh = ddiv<EXACT>(rz, h);
+    const double arg = mul<EXACT>(zh, zh);
     double dens;
     if (0.1 < r) {
-        dens = g.rho[0] * pow(r, g.rho[1]) * exp(-arg);
+        dens = mul<EXACT>(mul<EXACT>(g.rho[0], dpow<EXACT>(r, g.rho[1])), dexp<EXACT>(-arg));
     } else {
-        const double a = g.rho[0] * pow(0.1, g.rho[1] - 4.0);
-        dens = a * (r * r) * (r * r) * exp(-arg);
+        const double a = mul<EXACT>(g.rho[0], dpow<EXACT>(0.1, sub<EXACT>(g.rho[1], 4.0)));
+        const double r2 = mul<EXACT>(r, r);
+        dens = mul<EXACT>(mul<EXACT>(a, mul<EXACT>(r2, r2)), dexp<EXACT>(-arg));
     }
-    const double ux = gx - vx, uy = gy - vy, uz = 0.0 - vz;
-    const double un = sqrt(ux * ux + uy * uy + uz * uz);
-    f = decr * (3.0 * cd * dens * un) / (8.0 * radius * density);
+    const double ux = sub<EXACT>(gx, vx), uy = sub<EXACT>(gy, vy), uz = sub<EXACT>(0.0, vz);
+    const double un =
+        dsqrt<EXACT>(add<EXACT>(add<EXACT>(mul<EXACT>(ux, ux), mul<EXACT>(uy, uy)), mul<EXACT>(uz, uz)));
+    f = ddiv<EXACT>(mul<EXACT>(decr, mul<EXACT>(mul<EXACT>(mul<EXACT>(3.0, cd), dens), un)),
+                    mul<EXACT>(mul<EXACT>(8.0, radius), density));
 }
 
 // The same drag for the FP32 modes, with the transcendental factors in FP32.

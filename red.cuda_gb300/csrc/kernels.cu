@@ -71,7 +71,11 @@ __global__ void k_control(const ControlParams P)
             S.active = 0;
             return;
         }
-        if (0.0 < max_err) dt_new = dt * (0.9 * pow(P.tolerance / max_err, 1.0 / (double)P.order));
+        // the red-exact mode takes the nearest double of the power, as the C
+        // library's pow of red's host controller does (crmath.cuh)
+        if (0.0 < max_err)
+            dt_new = dt * (0.9 * (P.exact ? crmath::cr_pow(P.tolerance / max_err, 1.0 / (double)P.order)
+                                          : pow(P.tolerance / max_err, 1.0 / (double)P.order)));
         else dt_new = dt * 2.0;
         if (max_err > P.tolerance) {
             S.dt_try = dt_new;

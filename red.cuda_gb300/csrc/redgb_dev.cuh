@@ -196,6 +196,7 @@ struct ControlParams {
     int n_sys;
     int scheme, adaptive, order;
     int keep_dt;          // Euler / RK2: every step takes the initial dt (the dt_next clamp does not feed back)
+    int exact;            // red-exact mode: the step-size power rounded to the nearest double
     double tolerance, lambda;
     double output_interval, length;
     DevSys* sys;

@@ -921,6 +921,7 @@ void red_sim::enqueue_try(std::vector<int>* kinds, std::vector<cudaEvent_t>* evs
     C.adaptive = cfg.adaptive;
     C.order = order;
     C.keep_dt = (scheme == SCHEME_EULER || scheme == SCHEME_RK2) ? 1 : 0;
+    C.exact = mode == MODE_FP64_EXACT ? 1 : 0;
     C.tolerance = cfg.tolerance;
     C.lambda = lambda;
     C.output_interval = cfg.output_interval;

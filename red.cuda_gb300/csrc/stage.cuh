@@ -532,7 +532,7 @@ __global__ void __launch_bounds__(kTile, VT >= 0 ? 7 : 6) k_stage(const StagePar
     if (drag_on) {
         const double ts = P.standalone ? P.t_standalone
                                        : tsys + stage_c(P.scheme, s) * dt;
-        decr = gas_reduction_factor(P.gas, ts);
+        decr = gas_reduction_factor<EXACT>(P.gas, ts);
     }
     const bool drag_act = drag_on && !(1.0e-6 > decr);
     if (drag_act && t < it.nsink) {
@@ -544,8 +544,8 @@ __global__ void __launch_bounds__(kTile, VT >= 0 ? 7 : 6) k_stage(const StagePar
             drag_factor_fast(P.gas, decr, P.mass[it.soff], rb[0], rb[1], rb[2], vb[0], vb[1], vb[2], P.cd[ib],
                              P.radius[ib], P.density[ib], f, gx, gy);
         else
-            drag_factor(P.gas, decr, P.mass[it.soff], rb[0], rb[1], rb[2], vb[0], vb[1], vb[2], P.cd[ib],
-                        P.radius[ib], P.density[ib], f, gx, gy);
+            drag_factor<EXACT>(P.gas, decr, P.mass[it.soff], rb[0], rb[1], rb[2], vb[0], vb[1], vb[2], P.cd[ib],
+                               P.radius[ib], P.density[ib], f, gx, gy);
         sm.sc[t][0] = f;
         sm.sc[t][1] = gx;
         sm.sc[t][2] = gy;
@@ -694,7 +694,7 @@ __global__ void __launch_bounds__(kTile, VT >= 0 ? 7 : 6) k_stage(const StagePar
     if (!(idi > 0)) a = 0.0;   // calc_grav_accel_naive zeroes inactive sinks (pp_disk.cu:386-388)
     if (drag_act) {
         const double g = ce == 0 ? sm.sc[ke][1] : (ce == 1 ? sm.sc[ke][2] : 0.0);
-        a += sm.sc[ke][0] * (g - vs);
+        a = add<EXACT>(a, mul<EXACT>(sm.sc[ke][0], sub<EXACT>(g, vs)));   // a[i] += f u (pp_disk.cu:516-518)
     }
     P.Kv[s][x] = a;
 
