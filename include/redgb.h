@@ -194,9 +194,26 @@ int red_set_dt_next(red_sim* sim, uint32_t sys, double dt_next);
  * pp_disk.cu:1370-1430). */
 int red_rebuild_vectors(red_sim* sim);
 
-/* Times candidate gravity tilings on the current state and keeps the fastest
- * (red's own n_tpb search: pp_disk::benchmark, pp_disk.cu:553-611). */
+/* Times candidate launch plans (threads per sink group; source chunks from
+ * the planner's heuristic with or without the thread-block-cluster reduction,
+ * or fixed chunk sizes) by integrating real tries of the captured graph from
+ * a snapshot of the current state, keeps the fastest plan and restores the
+ * state, so the systems are left exactly where they were (red's own n_tpb
+ * search: pp_disk::benchmark, pp_disk.cu:553-611).  The red-exact mode has a
+ * single plan and is left as it is. */
 int red_autotune(red_sim* sim);
+/* The plan in use and what the last red_autotune measured (no counterpart in
+ * red, whose launch parameter is the single n_tpb, pp_disk.h:32-33). */
+typedef struct {
+    int32_t chunk;                /* sources per chunk (0: the planner's heuristic) */
+    int32_t lanes_cap;            /* largest threads per sink group */
+    int32_t cluster;              /* chunk sums reduced within thread-block clusters */
+    int32_t n_items;              /* stage-kernel CTAs of one launch */
+    int32_t candidates;           /* plans timed by the last red_autotune (0: none) */
+    float ms_per_try;             /* its best try time */
+    float ms_per_try_default;     /* its try time of the heuristic plan */
+} red_plan_info_t;
+int red_get_plan_info(red_sim* sim, red_plan_info_t* out);
 
 /* Runs one try launch by launch (outside the graph) with a CUDA event after
  * every kernel: ms[k] is the duration of launch k and kind[k] its kernel

@@ -439,6 +439,8 @@ struct red_sim {
     int chunk_override = 0;     // sources per chunk chosen by the autotuner (0 = heuristic)
     bool use_cluster = false;   // the plan's items are laid out for a cluster launch
     int lanes_cap = 32;         // upper bound on threads per sink (autotuner)
+    bool allow_cluster = true;  // the planner may lay chunk groups out as clusters (autotuner)
+    red_plan_info_t plan_info{};   // what the last red_autotune measured
 
     cudaGraphExec_t graph = nullptr;
     int launches_per_try = 0;
@@ -752,7 +754,8 @@ void red_sim::build_plan()
     if (!item_begin.empty()) item_begin[n_sys] = items.size();
     use_cluster = false;
     const char* cenv = getenv("REDGB_CLUSTER");
-    if ((mode == MODE_MIXED || mode == MODE_FP32) && chunk_override == 0 && !(cenv && cenv[0] == '0')) {
+    if ((mode == MODE_MIXED || mode == MODE_FP32) && chunk_override == 0 && allow_cluster &&
+        !(cenv && cenv[0] == '0')) {
         std::vector<GravItem> groups, singles;
         int max_chunk = 0;
         for (uint32_t s = 0; s < n_sys; s++)
@@ -2083,43 +2086,126 @@ int red_autotune(red_sim* sim)
 {
     if (int rc = check_sim(sim)) return rc;
     GUARD_BEGIN
-    // candidate source chunk sizes; the stage-0 gravity launch is timed on the
-    // current state (standalone, so nothing is integrated)
-    const int cands[] = {0, 128, 256, 512, 1024, 2048, 4096};
-    float best = 1e30f;
-    int best_c = 0;
+    // Candidate plans: threads per sink group (lanes_cap), and source chunks
+    // from the planner's heuristic (with or without the cluster reduction) or
+    // fixed sizes.  Each candidate integrates real tries (the whole captured
+    // graph) from a snapshot of the live state, which is restored afterwards:
+    // the systems end exactly where they were.  red's own precedent times its
+    // gravity kernel over thread-per-block counts (pp_disk.cu:553-611).
+    CK(cudaStreamSynchronize(sim->stream));
+    red_plan_info_t& info = sim->plan_info;
+    info.candidates = 0;
+    if (sim->mode == MODE_FP64_EXACT) {   // one lane per sink in red's order: nothing to choose
+        info.chunk = sim->chunk_override;
+        info.lanes_cap = sim->lanes_cap;
+        info.cluster = sim->use_cluster ? 1 : 0;
+        info.n_items = (int32_t)sim->items.size();
+        return RED_OK;
+    }
+    const size_t N = sim->n_cap;
+    double* s_r = dalloc<double>(3 * N);
+    double* s_v = dalloc<double>(3 * N);
+    DevSys* s_sys = dalloc<DevSys>(sim->n_sys);
+    unsigned int* s_nev = dalloc<unsigned int>(1);
+    float* s_feat = nullptr;
+    int* s_has = nullptr;
+    unsigned int* s_logn = nullptr;
+    cudaStream_t st = sim->stream;
+    auto copy = [&](void* dst, const void* src, size_t bytes) {
+        CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st));
+    };
+    auto swap_state = [&](bool save) {
+        auto mv = [&](void* live, void* saved, size_t bytes) { save ? copy(saved, live, bytes) : copy(live, saved, bytes); };
+        mv(sim->y_r, s_r, 3 * N * sizeof(double));
+        mv(sim->y_v, s_v, 3 * N * sizeof(double));
+        mv(sim->d_sys, s_sys, sim->n_sys * sizeof(DevSys));
+        mv(sim->d_nev, s_nev, sizeof(unsigned int));
+        if (s_feat) mv(sim->d_feat_prev, s_feat, (size_t)sim->n_sys * kFeat * sizeof(float));
+        if (s_has) mv(sim->d_has_prev, s_has, sim->n_sys * sizeof(int));
+        if (s_logn) mv(sim->d_log_n, s_logn, sizeof(unsigned int));
+    };
+    if (sim->d_feat_prev) s_feat = dalloc<float>((size_t)sim->n_sys * kFeat);
+    if (sim->d_has_prev) s_has = dalloc<int>(sim->n_sys);
+    if (sim->d_log_n) s_logn = dalloc<unsigned int>(1);
+    swap_state(true);
+    const bool ejhc_done = sim->ejhc_initial_done;   // the first try's ejection check is still owed
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    CK(cudaStreamSynchronize(sim->stream));
-    sim->prep_positions();
-    for (int c : cands) {
-        if (sim->mode == MODE_FP64_EXACT && c) continue;
-        sim->chunk_override = c;
+    struct Cand { int chunk, lanes; bool cluster; };
+    std::vector<Cand> cands;
+    for (int lanes : {32, 16, 8}) {
+        cands.push_back({0, lanes, true});
+        cands.push_back({0, lanes, false});
+        for (int c : {256, 512, 1024, 2048}) cands.push_back({c, lanes, false});
+    }
+    float best = 1e30f;
+    Cand best_c = cands[0];
+    int reps = 0;
+    for (const Cand& c : cands) {
+        sim->chunk_override = c.chunk;
+        sim->lanes_cap = c.lanes;
+        sim->allow_cluster = c.cluster;
         sim->build_plan();
-        StageParams P = sim->stage_params(0, true);
-        for (int w = 0; w < 2; w++) launch_stage(P, (int)sim->items.size(), sim->mode, sim->stream);
-        CK(cudaEventRecord(e0, sim->stream));
-        const int reps = 5;
-        for (int w = 0; w < reps; w++) launch_stage(P, (int)sim->items.size(), sim->mode, sim->stream);
-        CK(cudaEventRecord(e1, sim->stream));
+        if (c.cluster && !sim->use_cluster && c.chunk == 0) continue;   // same plan as the next candidate
+        sim->prep_positions();
+        sim->launch_tries(2);                  // graph capture, warm caches
+        if (reps == 0) {
+            CK(cudaEventRecord(e0, st));
+            sim->launch_tries(3);
+            CK(cudaEventRecord(e1, st));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            reps = std::max(3, std::min(50, (int)ceil(2.0 / std::max(ms / 3.0f, 1e-3f))));
+        }
+        CK(cudaEventRecord(e0, st));
+        sim->launch_tries((uint32_t)reps);
+        CK(cudaEventRecord(e1, st));
         CK(cudaEventSynchronize(e1));
-        sim->launches += 2 + reps;
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, e0, e1));
+        ms /= (float)reps;
+        if (info.candidates == 0) info.ms_per_try_default = ms;
+        info.candidates++;
         if (ms < best) {
             best = ms;
             best_c = c;
         }
+        swap_state(false);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    sim->chunk_override = best_c;
+    sim->chunk_override = best_c.chunk;
+    sim->lanes_cap = best_c.lanes;
+    sim->allow_cluster = best_c.cluster;
     sim->build_plan();
+    swap_state(false);
+    sim->ejhc_initial_done = ejhc_done;
     sim->prep_positions();
-    CK(cudaStreamSynchronize(sim->stream));
+    CK(cudaStreamSynchronize(st));
+    cudaFree(s_r); cudaFree(s_v); cudaFree(s_sys); cudaFree(s_nev);
+    cudaFree(s_feat); cudaFree(s_has); cudaFree(s_logn);
+    info.chunk = sim->chunk_override;
+    info.lanes_cap = sim->lanes_cap;
+    info.cluster = sim->use_cluster ? 1 : 0;
+    info.n_items = (int32_t)sim->items.size();
+    info.ms_per_try = best;
     return RED_OK;
     GUARD_END
+}
+
+int red_get_plan_info(red_sim* sim, red_plan_info_t* out)
+{
+    if (int rc = check_sim(sim)) return rc;
+    if (!out) return set_error(RED_ERR_ARG, "null argument");
+    red_plan_info_t i = sim->plan_info;
+    i.chunk = sim->chunk_override;
+    i.lanes_cap = sim->lanes_cap;
+    i.cluster = sim->use_cluster ? 1 : 0;
+    i.n_items = (int32_t)sim->items.size();
+    *out = i;
+    return RED_OK;
 }
 
 

@@ -25,7 +25,7 @@ EXPORTS = ["red_create", "red_destroy", "red_step", "red_launch_tries", "red_syn
            "red_handle_events", "red_check_for_collision", "red_check_for_ejection_hit_centrum",
            "red_calc_dydx", "red_calc_integral", "red_calc_energy_interacting", "red_get_state",
            "red_set_state", "red_get_states", "red_set_states", "red_get_system_info", "red_set_dt_next", "red_rebuild_vectors",
-           "red_autotune", "red_profile_try", "red_interactions_per_eval", "red_kernel_launches", "red_n_systems",
+           "red_autotune", "red_get_plan_info", "red_profile_try", "red_interactions_per_eval", "red_kernel_launches", "red_n_systems",
            "red_n_bodies",
            "red_calc_accel_noalloc", "red_mlp_param_count", "red_mlp_predict", "red_mlp_grad", "red_mlp_adam",
            "red_set_step_proposer", "red_clear_step_proposer", "red_log_features", "red_get_feature_log",
@@ -73,6 +73,12 @@ class AccelArgs(C.Structure):
 
 
 NOALLOC_MAX_BODIES = 32768
+
+
+class PlanInfo(C.Structure):
+    """red_plan_info_t: the launch plan in use and the last autotune's timings."""
+    _fields_ = [("chunk", C.c_int32), ("lanes_cap", C.c_int32), ("cluster", C.c_int32), ("n_items", C.c_int32),
+                ("candidates", C.c_int32), ("ms_per_try", C.c_float), ("ms_per_try_default", C.c_float)]
 
 
 class DiskSpec(C.Structure):
@@ -129,6 +135,7 @@ def load(path=LIB_PATH):
     L.red_set_dt_next.argtypes = [P, C.c_uint32, C.c_double]
     L.red_rebuild_vectors.argtypes = [P]
     L.red_autotune.argtypes = [P]
+    L.red_get_plan_info.argtypes = [P, C.POINTER(PlanInfo)]
     L.red_profile_try.argtypes = [P, P, P, C.c_uint32, u32p]
     L.red_interactions_per_eval.argtypes = [P]
     L.red_interactions_per_eval.restype = C.c_uint64
@@ -403,7 +410,17 @@ class Sim:
         _check(load().red_rebuild_vectors(self.h))
 
     def autotune(self):
+        """red_autotune: picks the fastest launch plan on the live state (which
+        it leaves unchanged); returns the plan and the measured try times."""
         _check(load().red_autotune(self.h))
+        return self.plan_info()
+
+    def plan_info(self):
+        i = PlanInfo()
+        _check(load().red_get_plan_info(self.h, C.byref(i)))
+        return {"chunk": i.chunk, "lanes_cap": i.lanes_cap, "cluster": bool(i.cluster), "n_items": i.n_items,
+                "candidates": i.candidates, "ms_per_try": i.ms_per_try,
+                "ms_per_try_default": i.ms_per_try_default}
 
     def set_step_proposer(self, w_bf16, norm, safety=1.0, ratio_lo=0.5, ratio_hi=2.0):
         """Enables the learned proposals: w_bf16 (np.uint16, mlp_param_count()), norm (MlpNorm)."""

@@ -5,7 +5,8 @@ The ensemble (independent disks, each with its own step size) partitions
 with no exchange between ranks: rank r owns systems [r * n, (r + 1) * n) of
 the seeded ensemble, so per-GPU work stays fixed as ranks are added (weak
 scaling).  A single disk does not shard; every rank integrates a replica.
-The only collective is the maximum of the ranks' timed durations.
+The only collectives are the maximum of the ranks' timed durations and the
+sum of the work they did.
 """
 
 
@@ -25,6 +26,18 @@ def max_over_ranks(value, device=None):
         return float(value)
     t = torch.tensor([float(value)], dtype=torch.float64, device=device or "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(value, device=None):
+    """Sum of a float over all ranks of the default process group (the value
+    itself without one): the work every rank did in the timed region."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device or "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
 
 
