@@ -15,8 +15,10 @@
 //             [-prec mixed|fp64|fp64_exact|fp32]
 //
 // -cpu, -gpu and -n_chg are accepted and ignored: the integration always runs
-// on the GPU.  Euler, RK2 and the FARGO gas disk (-gf) are not on this path
-// and are refused.
+// on the GPU.  Every integrator of red's parameter file is taken (Euler and
+// RK2 at the fixed initial step, as red's constructors).  The FARGO gas disk
+// (-gf) is refused, as red's own constructor fails on it
+// (fargo_gas_disk.cu:35, 259-261).
 #include <chrono>
 #include <cmath>
 #include <cstdint>
@@ -86,29 +88,50 @@ std::string read_text(const std::string& path)
     return ss.str();
 }
 
-// "key = value" lines (parameter.cpp:60-100; the analytic gas disk file alike)
+// Tokens of s between any of the delimiter characters, empty ones skipped
+// (the Tokenizer red's parsers use, red.cuda.utility/tokenizer.cpp:60-85).
+std::vector<std::string> tokens(const std::string& s, const char* delims)
+{
+    std::vector<std::string> out;
+    size_t i = 0;
+    while (i < s.size()) {
+        while (i < s.size() && strchr(delims, s[i])) i++;
+        size_t j = i;
+        while (j < s.size() && !strchr(delims, s[j])) j++;
+        if (j > i) out.push_back(s.substr(i, j - i));
+        i = j;
+    }
+    return out;
+}
+
+std::string lower(std::string s)
+{
+    for (char& c : s) c = (char)tolower((unsigned char)c);
+    return s;
+}
+
+// "key = value" lines as parameter::parse / set_param read them
+// (parameter.cpp:60-100, 108-112; analytic_gas_disk.cu:50-97 alike): every
+// non-empty line must hold a key and a value separated by '=', else the file
+// is rejected; the key is trimmed and lower-cased, the value trimmed.
 std::vector<std::pair<std::string, std::string>> key_values(const std::string& text)
 {
     std::vector<std::pair<std::string, std::string>> kv;
-    std::istringstream in(text);
-    std::string line;
-    while (std::getline(in, line)) {
-        const size_t hash = line.find('#');
-        if (hash != std::string::npos) line = line.substr(0, hash);
-        const size_t eq = line.find('=');
-        if (eq == std::string::npos) continue;
-        const std::string k = trim(line.substr(0, eq)), v = trim(line.substr(eq + 1));
-        if (!k.empty()) kv.emplace_back(k, v);
+    for (const std::string& line : tokens(text, "\r\n")) {
+        const std::vector<std::string> t = tokens(line, "=");
+        if (t.size() < 2) throw Fail{"Invalid key/value pair: " + line + "."};
+        kv.emplace_back(lower(trim(t[0])), trim(t[1]));
     }
     return kv;
 }
 
+// tools::is_number (tools.cpp:29-43) then atof, as red reads its numbers
 double number(const std::string& key, const std::string& v)
 {
-    char* end = nullptr;
-    const double x = strtod(v.c_str(), &end);
-    if (v.empty() || *end != '\0') throw Fail{"Invalid number at: " + key};
-    return x;
+    for (char c : v)
+        if (!(isdigit((unsigned char)c) || c == 'e' || c == 'E' || c == '.' || c == '-' || c == '+'))
+            throw Fail{"Invalid number at: " + key};
+    return atof(v.c_str());
 }
 
 // parameter::set_param (parameter.cpp:108-240) and transform_time (:250-257)
@@ -119,15 +142,17 @@ Param read_param(const std::string& path)
         if (key == "name") p.name = value;
         else if (key == "description") p.desc = value;
         else if (key == "output data representation" || key == "odr") {
-            if (value == "t" || value == "text") p.binary = false;
-            else if (value == "b" || value == "binary") p.binary = true;
-            else throw Fail{"Invalid data representation: " + value};
+            const std::string lv = lower(value);
+            if (lv == "t" || lv == "text") p.binary = false;
+            else if (lv == "b" || lv == "binary") p.binary = true;
+            else throw Fail{"Invalid data type: " + lv};
         } else if (key == "integrator") {
-            if (value == "euler" || value == "e") p.integrator = RED_INTEGRATOR_EULER;
-            else if (value == "runge-kutta2" || value == "rk2") p.integrator = RED_INTEGRATOR_RUNGEKUTTA2;
-            else if (value == "runge-kutta4" || value == "rk4") p.integrator = RED_INTEGRATOR_RUNGEKUTTA4;
-            else if (value == "runge-kutta-fehlberg8" || value == "rkf8") p.integrator = RED_INTEGRATOR_RUNGEKUTTAFEHLBERG78;
-            else throw Fail{"Invalid integrator type: " + value};
+            const std::string lv = lower(value);
+            if (lv == "euler" || lv == "e") p.integrator = RED_INTEGRATOR_EULER;
+            else if (lv == "runge-kutta2" || lv == "rk2") p.integrator = RED_INTEGRATOR_RUNGEKUTTA2;
+            else if (lv == "runge-kutta4" || lv == "rk4") p.integrator = RED_INTEGRATOR_RUNGEKUTTA4;
+            else if (lv == "runge-kutta-fehlberg8" || lv == "rkf8") p.integrator = RED_INTEGRATOR_RUNGEKUTTAFEHLBERG78;
+            else throw Fail{"Invalid integrator type: " + lv};
         } else if (key == "tolerance") {
             p.tolerance = number(key, value);
             p.adaptive = true;
@@ -143,7 +168,7 @@ Param read_param(const std::string& path)
         else if (key == "hit centrum") p.threshold[RED_THRESHOLD_HIT_CENTRUM_DISTANCE] = number(key, value);
         else if (key == "radii enhance factor" || key == "collision factor")
             p.threshold[RED_THRESHOLD_RADII_ENHANCE_FACTOR] = number(key, value);
-        else throw Fail{"Invalid parameter: " + key};
+        else throw Fail{"Invalid parameter: " + key + "."};
     }
     return p;
 }
@@ -158,12 +183,12 @@ red_gas_params_t read_gas(const std::string& path)
     const double gcm3 = gram_to_solar / (cm_au * cm_au * cm_au);
     const double kday = kYearToDay * kGauss;
     for (const auto& [key, value] : key_values(read_text(path))) {
-        if (key == "name") continue;
+        if (key == "name" || key == "description") continue;
         if (key == "time_dependence") {
             if (value == "constant" || value == "const") g.gas_decrease = 0;
             else if (value == "linear" || value == "lin") g.gas_decrease = 1;
             else if (value == "exponential" || value == "exp") g.gas_decrease = 2;
-            else throw Fail{"Invalid time dependence: " + value};
+            else throw Fail{"Invalid value at: " + key + "."};
             continue;
         }
         const double x = number(key, value);
@@ -181,7 +206,7 @@ red_gas_params_t read_gas(const std::string& path)
         else if (key == "t0") g.t0 = x * kday;
         else if (key == "t1") g.t1 = x * kday;
         else if (key == "e_folding_time") g.e_folding_time = x * kday;
-        else throw Fail{"Invalid gas disk parameter: " + key};
+        else throw Fail{"Invalid parameter :" + key + "."};
     }
     return g;
 }
@@ -446,8 +471,6 @@ struct Run {
     {
         wall0 = now();
         par = read_param(path_join(opt.idir, opt.param));
-        if (par.integrator != RED_INTEGRATOR_RUNGEKUTTA4 && par.integrator != RED_INTEGRATOR_RUNGEKUTTAFEHLBERG78)
-            throw Fail{"only the rk4 and rkf8 integrators are on this path"};
         // start files: the info record on line 1, the body records on line 2 (main.cu:206-214)
         std::istringstream sf(read_text(path_join(opt.idir, opt.start)));
         std::string fn_info, fn_data;

@@ -85,13 +85,22 @@ def write_system(dirname, stem, sysm, t=0.0, dt=0.0, dt_cpu=0, binary=False):
 
 
 def read_info(path):
+    """(t, dt, dt_CPU, counts[7]) of an info record; ValueError on a short or
+    malformed record (red's reader would read garbage, file_util.cpp:325-353)."""
     if path.endswith(".dat"):
         with open(path, "rb") as f:
             raw = f.read(48)
+        if len(raw) < 48:
+            raise ValueError("%s: binary info record of %d bytes, expected 48" % (path, len(raw)))
         t, dt, dt_cpu, *counts = struct.unpack("<ddI7I", raw)
         return t, dt, dt_cpu, np.array(counts, np.uint32)
     tok = open(path).read().split()
-    return float(tok[0]), float(tok[1]), int(tok[2]), np.array([int(x) for x in tok[3:10]], np.uint32)
+    if len(tok) < 10:
+        raise ValueError("%s: info record of %d fields, expected 10" % (path, len(tok)))
+    try:
+        return float(tok[0]), float(tok[1]), int(tok[2]), np.array([int(x) for x in tok[3:10]], np.uint32)
+    except ValueError as e:
+        raise ValueError("%s: malformed info record (%s)" % (path, e)) from None
 
 
 def read_data(path, n):
@@ -103,6 +112,8 @@ def read_data(path, n):
     if path.endswith(".dat"):
         raw = open(path, "rb").read()
         rec = 134
+        if len(raw) < rec * n:
+            raise ValueError("%s: %d bytes hold %d of the %d body records" % (path, len(raw), len(raw) // rec, n))
         for i in range(n):
             b = raw[i * rec:(i + 1) * rec]
             names.append(b[:30].split(b"\0")[0].decode())
@@ -113,13 +124,18 @@ def read_data(path, n):
             v[i] = (x[3], x[4], x[5], 0.0)
     else:
         tok = open(path).read().split()
+        if len(tok) < 15 * n:
+            raise ValueError("%s: %d fields hold %d of the %d body records" % (path, len(tok), len(tok) // 15, n))
         for i in range(n):
             f = tok[i * 15:(i + 1) * 15]
             names.append(f[0][:30])
-            md[i] = (int(f[1]), int(f[2]), int(f[3]), float(f[4]))
-            p[i] = tuple(float(x) for x in f[5:9])
-            r[i] = (float(f[9]), float(f[10]), float(f[11]), 0.0)
-            v[i] = (float(f[12]), float(f[13]), float(f[14]), 0.0)
+            try:
+                md[i] = (int(f[1]), int(f[2]), int(f[3]), float(f[4]))
+                p[i] = tuple(float(x) for x in f[5:9])
+                r[i] = (float(f[9]), float(f[10]), float(f[11]), 0.0)
+                v[i] = (float(f[12]), float(f[13]), float(f[14]), 0.0)
+            except ValueError as e:
+                raise ValueError("%s: malformed body record %d (%s)" % (path, i, e)) from None
     return r, v, p, md, names
 
 

@@ -49,10 +49,37 @@ def test_parameter_file_required(driver):
     assert p.returncode == 1 and "parameter file" in p.stderr
 
 
-def test_unsupported_integrator_refused(driver, rg, tmp_path):
-    write_case(rg, tmp_path, {"integrator": "e", "length": "0.01"})
+def write_param_text(d, text):
+    with open(os.path.join(str(d), "param.txt"), "w") as f:
+        f.write(text)
+
+
+def test_malformed_line_rejected(driver, rg, tmp_path):
+    """parameter::parse throws on a line without a key = value pair (parameter.cpp:96)."""
+    write_case(rg, tmp_path, {})
+    write_param_text(tmp_path, "integrator = rkf8\ntolerance 1e-10\n")
     p = run(driver, "-idir", str(tmp_path), "-odir", str(tmp_path), "-p", "param.txt")
-    assert p.returncode == 1 and "rk4 and rkf8" in p.stderr
+    assert p.returncode == 1 and "Invalid key/value pair: tolerance 1e-10." in p.stderr
+
+
+def test_invalid_number_rejected(driver, rg, tmp_path):
+    write_case(rg, tmp_path, {})
+    write_param_text(tmp_path, "tolerance = 1e-1O\n")
+    p = run(driver, "-idir", str(tmp_path), "-odir", str(tmp_path), "-p", "param.txt")
+    assert p.returncode == 1 and "Invalid number at: tolerance" in p.stderr
+
+
+@pytest.mark.parametrize("integrator", ["E", "Euler", "RK2", "Runge-Kutta4", "RKF8"])
+def test_keys_and_values_case_insensitive(driver, rg, tmp_path, integrator):
+    """Keys and the integrator / representation values are lower-cased as red
+    does (parameter.cpp:108, 120, 136); every integrator of red is taken.  The
+    parse comes before any device work: without a GPU the run stops later, at
+    the device, never at the parameter file."""
+    write_case(rg, tmp_path, {})
+    write_param_text(tmp_path, "Integrator = %s\nTOLERANCE = 1e-10\nLength = 0.001\nODR = Text\n" % integrator)
+    p = run(driver, "-idir", str(tmp_path), "-odir", str(tmp_path), "-p", "param.txt")
+    assert "Invalid" not in p.stderr, p.stderr
+    assert p.returncode == 0 or "device" in p.stderr.lower() or "cuda" in p.stderr.lower(), p.stderr
 
 
 def test_invalid_parameter_refused(driver, rg, tmp_path):
@@ -99,3 +126,27 @@ def test_driver_run_matches_library_and_restarts(driver, rg, tmp_path):
     assert len(snaps2) > len(snaps)
     n_last = int(snaps[-1][5:14])
     assert int(snaps2[len(snaps)][5:14]) == n_last + 1
+
+
+@pytest.mark.gpu
+def test_driver_euler_from_parameter_file(driver, rg, tmp_path):
+    """Euler chosen in the parameter file (upper case) runs at the fixed initial
+    step and ends where the library's red-exact Euler run ends, bit for bit."""
+    s = write_case(rg, tmp_path, {})
+    write_param_text(tmp_path, "INTEGRATOR = E\nlength = 0.002\nodr = text\n")
+    out = tmp_path / "out"
+    out.mkdir()
+    p = run(driver, "-idir", str(tmp_path), "-odir", str(out), "-p", "param.txt", "-prec", "fp64_exact")
+    assert p.returncode == 0, p.stderr
+    start = open(out / "start_files.txt").read().split()
+    final, t_final, _, _ = rg.redio.read_system(str(out), start[0], start[1])
+    K = rg.ic.K
+    with rg.Sim(s, integrator="euler", adaptive=False, dt=0.01, precision="fp64_exact",
+                length=0.002 * 365.25 * K) as sim:
+        while sim.info(0).active:
+            sim.step()
+        ref = sim.get_state(0)
+        t_ref = sim.info(0).t
+    assert t_final == t_ref
+    for f in "xyz":
+        assert np.array_equal(final.r[f], ref.r[f]) and np.array_equal(final.v[f], ref.v[f])
