@@ -217,6 +217,7 @@ def snapshot(sim):
     infos = [sim.info(k) for k in range(sim.n_systems)]
     return {"t": np.array([i.t for i in infos]), "tried": np.array([i.n_tried for i in infos], np.int64),
             "failed": np.array([i.n_failed for i in infos], np.int64),
+            "collisions": np.array([i.n_collision[0] for i in infos], np.int64),   # total (red_type.h:156)
             "ipe": np.array([ipe_of(list(i.playing)) for i in infos], np.int64)}
 
 
@@ -382,13 +383,15 @@ def settle(sim, tries):
         done += k
 
 
-def measure(torch, sim, stream, args, flush, steps, tps):
+def measure(torch, sim, stream, args, flush, steps, tps, stats=None):
     """Timed steps plus the work the tries did: (ms, interactions, sim-time, tries, failed)."""
     a = snapshot(sim)
     ms = timed_steps(torch, sim, stream, steps, flush, tps)
     drain_events(sim)
     b = snapshot(sim)
     tried = b["tried"] - a["tried"]
+    if stats is not None:
+        stats["collisions"] = int(np.sum(b["collisions"] - a["collisions"]))
     return ms, float(np.sum(b["ipe"] * tried)), float(np.sum(b["t"] - a["t"])), int(tried.sum()), \
         int(np.sum(b["failed"] - a["failed"]))
 
@@ -408,6 +411,7 @@ def plain_comparison(rg, systems, kw, args, local_rank, stream, flush, ns):
 
 def run_reference(args, rg, rank, world):
     systems, kw, desc = workload(rg, args.config)
+    kw, desc = with_tolerance(args, kw, desc)
     if rank != 0:
         return
     import oracle
@@ -426,11 +430,20 @@ def run_reference(args, rg, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def with_tolerance(args, kw, desc):
+    """--tolerance overrides the workload's RKF7(8) tolerance (named in the description)."""
+    if args.tolerance and kw.get("adaptive"):
+        kw = dict(kw, tolerance=args.tolerance)
+        desc = desc.replace("tol 1e-10", "tol %g" % args.tolerance)
+    return kw, desc
+
+
 def run_ours(args, rg, rank, world, local_rank):
     import torch
     torch.cuda.set_device(local_rank)
     t_ic = time.perf_counter()
     systems, kw, desc = workload(rg, args.config, rank, world)
+    kw, desc = with_tolerance(args, kw, desc)
     t_ic = time.perf_counter() - t_ic
     ic_gpu = None
     if args.config in ("c4", "c5"):
@@ -472,7 +485,8 @@ def run_ours(args, rg, rank, world, local_rank):
     clocks.start()
     rg.shard.barrier(local_rank)
     torch.cuda.synchronize()
-    ms, inter, sim_dt, tried, failed = measure(torch, sim, stream, args, flush, args.steps, tps)
+    stats = {}
+    ms, inter, sim_dt, tried, failed = measure(torch, sim, stream, args, flush, args.steps, tps, stats)
     torch.cuda.synchronize()
     rg.shard.barrier(local_rank)
     clk = clocks.stop()
@@ -558,6 +572,7 @@ def run_ours(args, rg, rank, world, local_rank):
                 "config": config_object(args, systems, kw, desc, world),
                 "sim_years_per_s": sim_years_all / (t_max * 1e-3),
                 "dE_over_E": dE,
+                "collisions_in_timed_region": stats.get("collisions"),
                 "tries_in_timed_region": int(tried),
                 "ms_per_try": ms_per_try,
                 "accept_fraction": (1.0 - failed / tried) if tried else None,
@@ -595,26 +610,30 @@ def run_ours(args, rg, rank, world, local_rank):
 
 def run_accuracy(args, rg, local_rank=0):
     """The accuracy statement: the 16384-body disk over T years (1000 orbits at
-    1 AU for T = 1000) in MIXED precision against this library's FP64 mode, the
-    same start and the same tolerance.  Collisions are off in both runs so
+    1 AU for T = 1000) in MIXED precision against this library's FP64 mode,
+    the same start and the same tolerance.  Collisions are off in both runs so
     that they integrate the same bodies (a merge changes E by design).  Each
     run stops past T and one fixed RKF7(8) step of the remaining (tiny) time
     brings it to T exactly, so positions compare at the same instant.
     Reported: |dE/E| (E over the interacting pairs), the relative drift of the
     angular momentum, and the relative position error of every body against
-    the FP64 run (median, 90th percentile, largest; the protoplanets apart)."""
+    the FP64 run (median, 90th percentile, largest; the protoplanets apart).
+    The disk is chaotic (close encounters), so a third run -- MIXED again,
+    from a start that differs by one ulp in one planetesimal's x -- measures
+    the divergence that any difference of rounding grows into over T: the
+    floor under which no precision can bring the position error."""
     import torch
     torch.cuda.set_device(local_rank)
     systems, kw, desc = workload(rg, "c2")
-    kw = dict(kw, collision_factor=0.0)
+    kw = dict(kw, collision_factor=0.0, tolerance=args.tolerance or kw["tolerance"])
     T = args.accuracy_years * YEAR * K_GAUSS
-    res = {}
-    for prec in ("mixed", "fp64"):
-        sim = rg.Sim(systems, precision=prec, length=T, device=local_rank, **kw)
+
+    def one(prec, s0):
+        sim = rg.Sim(s0, precision=prec, length=T, device=local_rank, **kw)
         E0 = sim.energy_interacting(0)
         t0 = time.perf_counter()
         while True:
-            sim.launch_tries(1000)
+            sim.launch_tries(2000)
             act, halted = sim.synchronize()
             if halted:
                 sim.handle_events()
@@ -633,22 +652,32 @@ def run_accuracy(args, rg, local_rank=0):
             E1 = s2.energy_interacting(0)
             fin = s2.get_state(0)
             t_end = s2.info(0).t
-        res[prec] = {"wall_s": wall, "tries": int(tried), "failed": int(failed), "t_end": t_end,
-                     "dE_over_E": abs((E1[0] - E0[0]) / E0[0]),
-                     "dC_over_C": float(np.linalg.norm(E1[1:] - E0[1:]) / np.linalg.norm(E0[1:])),
-                     "sim_years_per_s": args.accuracy_years / wall,
-                     "r": np.stack([fin.r["x"], fin.r["y"], fin.r["z"]], axis=1)}
-    a, b = res["mixed"]["r"], res["fp64"]["r"]
-    rel = np.linalg.norm(a - b, axis=1) / np.linalg.norm(b, axis=1)
-    n_si = systems[0].n_SI
+        return {"wall_s": wall, "tries": int(tried), "failed": int(failed), "t_end": t_end,
+                "dE_over_E": abs((E1[0] - E0[0]) / E0[0]),
+                "dC_over_C": float(np.linalg.norm(E1[1:] - E0[1:]) / np.linalg.norm(E0[1:])),
+                "sim_years_per_s": args.accuracy_years / wall,
+                "r": np.stack([fin.r["x"], fin.r["y"], fin.r["z"]], axis=1)}
+
+    s = systems[0]
+    res = {"mixed": one("mixed", s), "fp64": one("fp64", s)}
+    sp = s.copy()
+    k = s.n_SI + 100
+    sp.r["x"][k] = np.nextafter(sp.r["x"][k], np.inf)
+    res["mixed_1ulp"] = one("mixed", sp)
+    n_si = s.n_SI
+
+    def err(a, b):
+        rel = np.linalg.norm(a - b, axis=1) / np.linalg.norm(b, axis=1)
+        return {"median": float(np.median(rel[1:])), "p90": float(np.percentile(rel[1:], 90)),
+                "max": float(rel[1:].max()), "protoplanets_max": float(rel[1:n_si].max()),
+                "star_abs": float(np.linalg.norm(a[0] - b[0]))}
     out = {"accuracy": {
-        "workload": desc + "; collisions off", "years": args.accuracy_years, "tolerance": kw["tolerance"],
+        "workload": desc.replace(", collisions on", "") + ", collisions off", "years": args.accuracy_years,
+        "tolerance": kw["tolerance"],
         "reference": "this library's FP64 mode (FP64 pairs with FMA), same start, same tolerance",
-        "mixed": {k: v for k, v in res["mixed"].items() if k != "r"},
-        "fp64": {k: v for k, v in res["fp64"].items() if k != "r"},
-        "position_error_vs_fp64": {"median": float(np.median(rel[1:])), "p90": float(np.percentile(rel[1:], 90)),
-                                   "max": float(rel[1:].max()), "protoplanets_max": float(rel[1:n_si].max()),
-                                   "star": float(np.linalg.norm(a[0] - b[0]))}}}
+        "runs": {k: {q: v for q, v in r.items() if q != "r"} for k, r in res.items()},
+        "position_error_mixed_vs_fp64": err(res["mixed"]["r"], res["fp64"]["r"]),
+        "chaos_floor_mixed_1ulp_vs_mixed": err(res["mixed_1ulp"]["r"], res["mixed"]["r"])}}
     print(json.dumps(out), flush=True)
 
 
@@ -692,6 +721,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp32", "fp64_exact"])
     ap.add_argument("--tries-per-step", type=int, default=0)
     ap.add_argument("--accuracy-years", type=float, default=0.0)
+    ap.add_argument("--tolerance", type=float, default=0.0)
     ap.add_argument("--plan-only", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")

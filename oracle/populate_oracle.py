@@ -5,13 +5,16 @@ The generator follows red.cuda.initial's disk recipe (populate_disk,
 red.cuda.initial/main.cu:251-314; calculate_phase, main.cu:317-342;
 distribution.cpp:105-109 for the Rayleigh draws; tools.cpp:413-434, 455-472,
 716-749, 789-828 for the barycentre, radius / density, Kepler solver and
-Kepler -> Cartesian), with Philox4x32-10 (Salmon, Moraes, Dror and Shaw, "Parallel
+Kepler -> Cartesian; the Kepler solver is oracle/red_initial.py's, pinned to
+red's compiled generator), with Philox4x32-10 (Salmon, Moraes, Dror and Shaw, "Parallel
 random numbers: as easy as 1, 2, 3", SC'11) as the random source: key = the
 system's seed, counter = (body, draw block, 0, 0).  The integer stream is
 exact; the floating-point math uses numpy's libm, so results agree with the
 GPU's to rounding of the math functions (about 1e-15 relative).
 """
 import numpy as np
+
+from .red_initial import kepler_E   # red's solver, pinned to red.cuda.initial
 
 K = 0.01720209895
 K2 = 0.0002959122082855911025
@@ -58,17 +61,6 @@ def draws(seed, n):
         u[:, 2 * b] = u01(out[:, 0], out[:, 1])
         u[:, 2 * b + 1] = u01(out[:, 2], out[:, 3])
     return u
-
-
-def kepler_E(ecc, mean):
-    mean = np.fmod(mean, TWO_PI)
-    E = mean + ecc * np.sin(mean)
-    done = np.zeros(E.shape, bool)
-    for _ in range(30):
-        dE = (E - ecc * np.sin(E) - mean) / (1.0 - ecc * np.cos(E))
-        E = np.where(done, E, E - dE)
-        done |= np.abs(dE) < 1.0e-15
-    return E
 
 
 def populate(spec):

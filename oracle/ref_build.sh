@@ -54,3 +54,17 @@ done
 for p in "${pids[@]:-}"; do [ -n "$p" ] && wait "$p"; done
 $NVCC $FLAGS $INC -o "$OUT/ref_harness" "$HERE/ref_harness.cu" "${objs[@]}"
 echo "$OUT/ref_harness"
+# red.cuda.initial's generator (golden vectors of the disk recipe), when its
+# sources are there: the harness includes its main.cu with main() renamed
+INIT="$REF/src/red.cuda.initial"
+if [ -d "$INIT" ]; then
+  iobjs=()
+  for s in "$INIT/distribution.cpp" "$INIT/util_init.cpp" "$INIT/nebula.cpp"; do
+    o="$OUT/obj/init_$(basename "${s%.*}").o"
+    iobjs+=("$o")
+    [ -f "$o" ] && [ ! "$s" -nt "$o" ] || $NVCC -c $FLAGS -I"$INIT" $INC -x cu -o "$o" "$s"
+  done
+  $NVCC $FLAGS -I"$INIT" $INC -o "$OUT/initial_harness" "$HERE/initial_harness.cu" "${iobjs[@]}" \
+    "$OUT/obj/tools.o" "$OUT/obj/file_util.o" "$OUT/obj/util.o" "$OUT/obj/tokenizer.o"
+  echo "$OUT/initial_harness"
+fi

@@ -23,6 +23,7 @@ constexpr double kK = 0.01720209895;                 // red_macro.h:13
 constexpr double kK2 = 0.0002959122082855911025;     // red_macro.h:14
 constexpr double kFourPiOverThree = 4.188790204786391;   // tools.cpp:457
 constexpr double kTwoPi = 6.283185307179586;
+constexpr double kPi = 3.1415926535897932384626;   // red_macro.h:16
 constexpr int kPopBlock = 256;
 
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw: "Parallel random numbers: as easy
@@ -152,16 +153,24 @@ __global__ void __launch_bounds__(kPopBlock) k_pop_wsum(const PopParams P)
     if (threadIdx.x == 0) P.wsum[s] = tot;
 }
 
-// tools::kepler_equation_solver (tools.cpp:716-749): Newton from E = M + e sin M.
+// tools::kepler_equation_solver as calc_phase calls it (tools.cpp:715-755,
+// 789-795; tolerance 1e-8): Newton from red's starting value.  For a mean
+// anomaly above pi red's solver ends with E = (mean - pi) + pi, the mean
+// anomaly itself rather than the solution; that is kept, so that the disks
+// follow red's generator (the point is still on the orbit, at another phase).
 __device__ inline double kepler_E(double ecc, double mean)
 {
-    mean = fmod(mean, kTwoPi);
-    double E = mean + ecc * sin(mean);
-    for (int it = 0; it < 30; it++) {
-        const double dE = (E - ecc * sin(E) - mean) / (1.0 - ecc * cos(E));
-        E -= dE;
-        if (fabs(dE) < 1.0e-15) break;
+    if (ecc == 0.0 || mean == 0.0 || mean == kPi) return mean;
+    const bool s = kPi < mean;
+    if (s) mean -= kPi;
+    double E = mean + ecc * sin(mean) / (1.0 - sin(mean + ecc) + sin(mean));
+    for (int it = 0; it < 34; it++) {
+        const double E1 = E - (E - ecc * sin(E) - mean) / (1.0 - ecc * cos(E));
+        const double err = fabs(E1 - E);
+        E = E1;
+        if (!(err > 1.0e-8)) break;
     }
+    if (s) E += (mean - E) + kPi;
     return E;
 }
 

@@ -1,17 +1,20 @@
-"""Synthetic planetesimal disks built with the math of red's IC generator.
+"""Synthetic planetesimal disks built with red's IC generator's random source
+and recipe.
 
-Follows src/red.cuda.initial (populate_disk, main.cu:251-314; calculate_phase,
-main.cu:317-342; distribution.cpp:11-204): orbital elements drawn from
-uniform / Rayleigh / power-law distributions, Kepler elements converted to
-Cartesian coordinates with mu = K^2 (m_0 + m) (tools.cpp:789-828), then the
-system is moved to the barycentre (tools.cpp:413-434) and velocities are
-divided by k so that time is in red's code unit 1/k day
-(red.cuda.initial/main.cu:1666-1670).  Random numbers come from numpy's
-MT19937 bit generator with the stated seed (the generator is an input source,
-not part of the compared path).
+Follows src/red.cuda.initial: red_random and its distributions
+(distribution.cpp:11-204; every drawn quantity has its own MT19937 stream,
+seeded I[0] = seed), populate_disk (main.cu:251-314), calculate_phase
+(main.cu:317-342) with tools::calc_phase and kepler_equation_solver
+(tools.cpp:715-828: mu = K^2 (m_0 + m), red's solver and its tolerance),
+then transform_to_bc (tools.cpp:384-434) and velocities divided by k so that
+time is in red's code unit 1/k day (main.cu:2786-2790).  The disks' layouts
+(protoplanets at given semi-major axes, mass weights) are this project's
+workload definitions.
 
 Units: AU, M_sun, code time (1/k day).
 """
+import math
+
 import numpy as np
 
 from .types import (BMD, PARAM, PLANETESIMAL, PROTOPLANET, STAR, SUPERPLANETESIMAL, TESTPARTICLE,
@@ -32,6 +35,61 @@ _CM_AU = 1.0e-2 * METER_TO_AU
 G_CM3_TO_SOLAR_AU3 = GRAM_TO_SOLAR / (_CM_AU * _CM_AU * _CM_AU)   # red_constants.h:184
 YEAR_TO_DAY = 365.25
 FOUR_PI_OVER_THREE = 4.188790204786391  # tools.cpp:457
+PI = 3.1415926535897932384626           # red_macro.h:16
+
+
+class RedStreams:
+    """red's random source for one disk: the k-th quantity drawn gets its own
+    red_random stream (MT19937 seeded I[0] = seed, distribution.cpp:11-20,
+    the stream of numpy's MT19937 under its legacy integer seeding), seeded
+    64 seed + k, as red gives every distribution object its own seed.  The
+    formulas are red's: uniform(a, b) = a + (b - a)(rand() + 1) / 2^32
+    (distribution.cpp:36-44), Rayleigh sigma sqrt(-2 ln u) (:105-109), the
+    power law by rejection (:141-162) and integers by red_random::uniform(int)
+    (:46-49)."""
+
+    def __init__(self, seed):
+        self.seed = int(seed)
+        self.k = 0
+
+    def _raw(self, n):
+        bg = np.random.MT19937(0)
+        bg._legacy_seeding((64 * self.seed + self.k) & 0xFFFFFFFF)
+        self.k += 1
+        return bg.random_raw(n).astype(np.float64)
+
+    def uniform(self, lo, hi, n):
+        return lo + (hi - lo) * (self._raw(n) + 1.0) / 4294967296.0
+
+    def rayleigh(self, sigma, n):
+        u = (self._raw(n) + 1.0) / 4294967296.0
+        return np.fromiter((sigma * math.sqrt(-2.0 * math.log(x)) for x in u), float, n)
+
+    def power(self, lo, hi, power, n):
+        """power_law_distribution::get_next, n times: every attempt takes two
+        consecutive draws (x, then y), so the accepted values are the first n
+        accepted pairs of the stream."""
+        y_min = 0.0 if power == 0.0 else math.pow(lo, power)
+        y_max = 1.0 if power == 0.0 else math.pow(hi, power)
+        y_min, y_max = min(y_min, y_max), max(y_min, y_max)
+        d_y, d_x = y_max - y_min, hi - lo
+        area = d_x * d_y
+        bg = np.random.MT19937(0)
+        bg._legacy_seeding((64 * self.seed + self.k) & 0xFFFFFFFF)
+        self.k += 1
+        out = []
+        while len(out) < n:
+            raw = bg.random_raw(2 * max(1024, 4 * (n - len(out)))).astype(np.float64).reshape(-1, 2)
+            x = (0.0 + (area - 0.0) * (raw[:, 0] + 1.0) / 4294967296.0) / d_y + lo
+            y = y_min + (y_max - y_min) * (raw[:, 1] + 1.0) / 4294967296.0
+            ok = np.fromiter((not (yy > math.pow(xx, power)) for xx, yy in zip(x, y)), bool, len(x))
+            out.extend(x[ok][:n - len(out)])
+        return np.array(out[:n])
+
+    def integer(self, lo, hi):
+        """red_random::uniform(int x_min, int x_max): one value in [lo, hi]."""
+        r = self._raw(1)[0]
+        return lo + int(r / 4294967296. * (hi - lo + 1))
 
 
 def calc_radius(m, density):
@@ -46,17 +104,28 @@ def calc_density(m, R):
         return np.where(R == 0.0, 0.0, m / (FOUR_PI_OVER_THREE * R ** 3))
 
 
-def kepler_E(ecc, mean, iters=30):
-    """Eccentric anomaly from the mean anomaly (Newton's method, as
-    tools::kepler_equation_solver, tools.cpp:716-749)."""
-    mean = np.mod(mean, 2 * np.pi)
-    E = mean + ecc * np.sin(mean)
-    for _ in range(iters):
-        dE = (E - ecc * np.sin(E) - mean) / (1.0 - ecc * np.cos(E))
-        E = E - dE
-        if np.max(np.abs(dE), initial=0.0) < 1e-15:
+def kepler_E(ecc, mean):
+    """tools::kepler_equation_solver as calc_phase calls it (tools.cpp:715-755,
+    789-795; tolerance 1e-8, at most 34 Newton steps from red's starting
+    value), vectorised.  For a mean anomaly above pi red's solver ends with
+    E = (mean - pi) + pi -- the mean anomaly itself, not the solution -- and
+    so does this one, so that the disks are the ones red's generator makes."""
+    ecc = np.asarray(ecc, float)
+    mean = np.asarray(mean, float)
+    trivial = (ecc == 0.0) | (mean == 0.0) | (mean == PI)
+    upper = mean > PI
+    m = np.where(upper, mean - PI, mean)
+    E = m + ecc * np.sin(m) / (1.0 - np.sin(m + ecc) + np.sin(m))
+    settled = np.zeros(E.shape, bool)
+    for _ in range(34):
+        step = E - (E - ecc * np.sin(E) - m) / (1.0 - ecc * np.cos(E))
+        moved = np.abs(step - E)
+        E = np.where(settled, E, step)
+        settled |= moved <= 1.0e-8
+        if settled.all():
             break
-    return E
+    E = np.where(upper, E + ((m - E) + PI), E)
+    return np.where(trivial, mean, E)
 
 
 def calc_phase(mu, a, e, inc, peri, node, mean):
@@ -71,9 +140,19 @@ def calc_phase(mu, a, e, inc, peri, node, mean):
     cw, sw, cO, sO, ci, si = np.cos(peri), np.sin(peri), np.cos(node), np.sin(node), np.cos(inc), np.sin(inc)
     P = np.stack([cw * cO - sw * sO * ci, cw * sO + sw * cO * ci, sw * si], axis=1)
     Q = np.stack([-sw * cO - cw * sO * ci, -sw * sO + cw * cO * ci, cw * si], axis=1)
-    rv = ksi[:, None] * P + eta[:, None] * Q
-    vv = vk[:, None] * P + ve[:, None] * Q
+    rv = np.stack([ksi * P[:, c] + eta * Q[:, c] for c in range(3)], axis=1)
+    vv = np.stack([vk * P[:, c] + ve * Q[:, c] for c in range(3)], axis=1)
     return rv, vv
+
+
+def to_barycentre(mass, r, v):
+    """tools::transform_to_bc (tools.cpp:384-434): total mass and moments summed
+    from the last body to the first (sequential sums, as red's loop), then
+    subtracted; r and v are structured var4 arrays, updated in place."""
+    M = np.cumsum(mass[::-1])[-1]
+    for c in "xyz":
+        r[c] -= np.cumsum((mass * r[c])[::-1])[-1] / M
+        v[c] -= np.cumsum((mass * v[c])[::-1])[-1] / M
 
 
 def hill_spaced(a0, n, m, m_star, k_hill=10.0):
@@ -97,7 +176,7 @@ def build_system(rng, *, m_star=1.0, pp_a, pp_mass, pl_a, pl_mass, pl_radius=Non
     e = np.abs(np.concatenate([rng.rayleigh(sigma_e_pp, n_pp), rng.rayleigh(sigma_e, n_pl + n_tp)]))
     e = np.minimum(e, 0.9)
     inc = np.abs(np.concatenate([rng.rayleigh(sigma_i_pp, n_pp), rng.rayleigh(sigma_i, n_pl + n_tp)]))
-    peri, node, mean = (rng.uniform(0.0, 2 * np.pi, nb) for _ in range(3))
+    peri, node, mean = (rng.uniform(0.0, 2.0 * PI, nb) for _ in range(3))
     mu = K2 * (m_star + m)
     rv, vv = calc_phase(mu, a, e, inc, peri, node, mean)       # AU, AU/day
 
@@ -125,11 +204,7 @@ def build_system(rng, *, m_star=1.0, pp_a, pp_mass, pl_a, pl_mass, pl_radius=Non
     md["body_type"][1 + n_pp:1 + n_pp + n_pl] = pl_type
     md["body_type"][1 + n_pp + n_pl:] = TESTPARTICLE
 
-    # transform to the barycentre, tools::transform_to_bc (tools.cpp:413-434)
-    M = p["mass"].sum()
-    for c in "xyz":
-        r[c] -= (p["mass"] * r[c]).sum() / M
-        v[c] -= (p["mass"] * v[c]).sum() / M
+    to_barycentre(p["mass"], r, v)
     # velocities in AU per code time unit (1/k day)
     for c in "xyz":
         v[c] /= K
@@ -146,7 +221,7 @@ def build_system(rng, *, m_star=1.0, pp_a, pp_mass, pl_a, pl_mass, pl_radius=Non
 def config1(seed=1, n_pl=2048):
     """Star 1 M_sun, 4 protoplanets of 0.1 M_earth at 0.8-1.4 AU, n_pl equal-mass
     planetesimals (1 M_earth in total), a ~ U[0.7, 1.5], sigma_e 0.01, sigma_i 0.005."""
-    rng = np.random.Generator(np.random.MT19937(seed))
+    rng = RedStreams(seed)
     pl_a = rng.uniform(0.7, 1.5, n_pl)
     return build_system(rng, pp_a=np.array([0.8, 1.0, 1.2, 1.4]), pp_mass=0.1 * EARTH_TO_SOLAR,
                         pl_a=pl_a, pl_mass=EARTH_TO_SOLAR / n_pl)
@@ -156,9 +231,9 @@ def config2(seed=2, n_pp=16, n_pl=16367):
     """16 protoplanets of 0.05 M_earth spaced 10 mutual Hill radii from 0.5 AU;
     planetesimals log-uniform in [0.5, 3] AU with m ~ a^0.5 (surface density
     ~ r^-1.5), 1 M_earth in total; sigma_e 0.02, sigma_i 0.01."""
-    rng = np.random.Generator(np.random.MT19937(seed))
+    rng = RedStreams(seed)
     mpp = 0.05 * EARTH_TO_SOLAR
-    pl_a = np.exp(rng.uniform(np.log(0.5), np.log(3.0), n_pl))
+    pl_a = rng.power(0.5, 3.0, -1.0, n_pl)   # log-uniform: red's power law with power -1
     w = pl_a ** 0.5
     pl_m = EARTH_TO_SOLAR * w / w.sum()
     return build_system(rng, pp_a=hill_spaced(0.5, n_pp, mpp, 1.0), pp_mass=mpp, pl_a=pl_a, pl_mass=pl_m,
@@ -169,10 +244,10 @@ def config3(seed=3, n_pp=32, n_pl=65503):
     """32 protoplanets (0.05 M_earth, 10 mutual Hill radii from 0.5 AU) and
     planetesimals with a in [0.5, 4] AU and radii log-uniform in 1-100 km at
     2 g/cm^3, C_D = 0.44 (gas drag run)."""
-    rng = np.random.Generator(np.random.MT19937(seed))
+    rng = RedStreams(seed)
     mpp = 0.05 * EARTH_TO_SOLAR
     pl_a = rng.uniform(0.5, 4.0, n_pl)
-    R = np.exp(rng.uniform(np.log(1.0), np.log(100.0), n_pl)) / AU_TO_KM
+    R = rng.power(1.0, 100.0, -1.0, n_pl) / AU_TO_KM   # log-uniform radii
     return build_system(rng, pp_a=hill_spaced(0.5, n_pp, mpp, 1.0), pp_mass=mpp, pl_a=pl_a, pl_mass=0.0,
                         pl_radius=R, sigma_e_pp=0.01, sigma_i_pp=0.005, sigma_e=0.01, sigma_i=0.005,
                         cd=0.44)
@@ -181,9 +256,9 @@ def config3(seed=3, n_pp=32, n_pl=65503):
 def config4_system(i, n_min=128, n_max=4096):
     """System i of the ensemble: built like config 1 with its own seed
     (1000 + i), N ~ U[n_min, n_max] and 2-8 protoplanets."""
-    rng = np.random.Generator(np.random.MT19937(1000 + i))
-    n = int(rng.integers(n_min, n_max + 1))
-    n_pp = int(rng.integers(2, 9))
+    rng = RedStreams(1000 + i)
+    n = rng.integer(n_min, n_max)
+    n_pp = rng.integer(2, 8)
     n_pl = n - 1 - n_pp
     pp_a = 0.8 + 0.2 * np.arange(n_pp)
     pl_a = rng.uniform(0.7, 1.5, n_pl)
@@ -204,9 +279,9 @@ def config4_specs(n_systems=512, n_min=128, n_max=4096, first=0):
     from .lib import DiskSpec
     out = []
     for i in range(first, first + n_systems):
-        rng = np.random.Generator(np.random.MT19937(1000 + i))
-        n = int(rng.integers(n_min, n_max + 1))
-        n_pp = int(rng.integers(2, 9))
+        rng = RedStreams(1000 + i)
+        n = rng.integer(n_min, n_max)
+        n_pp = rng.integer(2, 8)
         n_pl = n - 1 - n_pp
         out.append(DiskSpec(n_pp=n_pp, n_pl=n_pl, m_star=1.0, star_radius=SOLAR_RADIUS_TO_AU,
                             pp_mass=0.1 * EARTH_TO_SOLAR, pp_a0=0.8, pp_da=0.2, pp_hill=0.0, pl_a_min=0.7,

@@ -6,7 +6,8 @@ red's input format, and stores inputs and the reference's outputs as .npz
 files.  Only needed when the fixtures are regenerated; the tests read the
 .npz files and never need the reference itself.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every fixture
+    python tests/golden/make_golden.py initial    # only the disk generator's
 """
 import os
 import shutil
@@ -211,11 +212,106 @@ def case_dump(tmp):
          names=np.array(s.names), **files)
 
 
-def main():
-    if not os.path.exists(HARNESS):
+INITIAL_SPECS = {
+    # star, 8 protoplanets (mass + density given: radius computed), 1000
+    # planetesimals (log-uniform a: red's power law with power -1; drag
+    # coefficient drawn), 20 test particles (exponential e, normal i)
+    "initial_disk.npz": """n 0 1
+pp 0 mass uniform 101 1.0 1.0
+pp 0 radius uniform 102 0.004649 0.004649
+pp 0 cd uniform 103 0.0 0.0
+n 3 8
+pp 3 mass uniform 111 1.0e-7 5.0e-7
+pp 3 density uniform 112 336.0 336.0
+oe 3 sma uniform 113 0.6 1.6
+oe 3 ecc rayleigh 114 0.02
+oe 3 inc rayleigh 115 0.01
+oe 3 peri uniform 116 0.0 6.283185307179586
+oe 3 node uniform 117 0.0 6.283185307179586
+oe 3 mean uniform 118 0.0 6.283185307179586
+n 5 1000
+pp 5 mass uniform 121 1.0e-10 4.0e-9
+pp 5 density uniform 122 200.0 500.0
+pp 5 cd uniform 123 0.3 0.6
+oe 5 sma power 124 0.5 3.0 -1.0
+oe 5 ecc rayleigh 125 0.02
+oe 5 inc rayleigh 126 0.01
+oe 5 peri uniform 127 0.0 6.283185307179586
+oe 5 node uniform 128 0.0 6.283185307179586
+oe 5 mean uniform 129 0.0 6.283185307179586
+n 6 20
+oe 6 sma uniform 131 0.7 1.5
+oe 6 ecc exponential 132 100.0
+oe 6 inc normal 133 0.0 0.01
+oe 6 peri uniform 134 0.0 6.283185307179586
+oe 6 node uniform 135 0.0 6.283185307179586
+oe 6 mean uniform 136 0.0 6.283185307179586
+""",
+    # the other fix-up branches: a giant planet with mass and radius given
+    # (density computed), planetesimals with radius and density given (mass
+    # computed), super-planetesimals (no fix-up) with all three given
+    "initial_branches.npz": """n 0 1
+pp 0 mass uniform 201 1.0 1.0
+pp 0 radius uniform 202 0.004649 0.004649
+n 1 2
+pp 1 mass uniform 211 9.0e-4 1.0e-3
+pp 1 radius uniform 212 4.0e-4 5.0e-4
+oe 1 sma uniform 213 4.0 6.0
+oe 1 ecc uniform 214 0.0 0.05
+oe 1 inc uniform 215 0.0 0.02
+oe 1 mean uniform 216 0.0 6.283185307179586
+n 4 30
+pp 4 mass uniform 221 1.0e-9 2.0e-9
+pp 4 radius uniform 222 1.0e-6 2.0e-6
+pp 4 density uniform 223 100.0 300.0
+oe 4 sma uniform 224 1.0 2.0
+oe 4 ecc rayleigh 225 0.05
+n 5 300
+pp 5 radius power 231 6.7e-9 6.7e-7 -1.0
+pp 5 density uniform 232 336.0 336.0
+pp 5 cd uniform 233 0.44 0.44
+oe 5 sma uniform 234 0.5 4.0
+oe 5 ecc rayleigh 235 0.01
+oe 5 inc rayleigh 236 0.005
+oe 5 peri uniform 237 0.0 6.283185307179586
+oe 5 node uniform 238 0.0 6.283185307179586
+oe 5 mean uniform 239 0.0 6.283185307179586
+""",
+}
+
+
+def case_initial(tmp):
+    """red.cuda.initial's own generator (oracle/_ref/initial_harness) on the specs above."""
+    harness = os.path.join(ROOT, "oracle", "_ref", "initial_harness")
+    for name, spec in INITIAL_SPECS.items():
+        path = os.path.join(tmp, "spec.txt")
+        open(path, "w").write(spec)
+        out = os.path.join(tmp, "init.bin")
+        subprocess.check_call([harness, path, out])
+        R = Reader(rd(out))
+        n = int(R.take("<u4")[0])
+        dt = float(R.take("<f8")[0])
+        r = R.take(rg.types.VAR4, n)
+        v = R.take(rg.types.VAR4, n)
+        p = R.take(rg.types.PARAM, n)
+        md = R.take(rg.types.BMD, n)
+        oe = R.take("<f8", 6 * n).reshape(n, 6)
+        save(name, spec=np.frombuffer(spec.encode(), np.uint8), dt=dt, r=r, v=v, p=p, md=md, oe=oe)
+
+
+CASES = ["accel", "drag", "runs", "collision", "ejhc", "integral", "dump", "initial"]
+
+
+def main(cases=None):
+    cases = cases or CASES
+    if not os.path.exists(HARNESS) or not os.path.exists(os.path.join(ROOT, "oracle", "_ref", "initial_harness")):
         subprocess.check_call([os.path.join(ROOT, "oracle", "ref_build.sh")])
     tmp = tempfile.mkdtemp(prefix="redgold")
     try:
+        if "initial" in cases:
+            case_initial(tmp)
+        if "accel" not in cases:
+            return
         case_accel(tmp)
         case_drag(tmp)
         case_run(tmp, "rk4_fixed", 4, 0, 0.0, 0.5, 40)
@@ -234,4 +330,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -203,3 +203,56 @@ def test_bounds(orc):
     assert orc.bound(pl, 2) == (21, 28, 0, 21)
     assert orc.bound(pl, 3) == (10, 21, 0, 0)
     assert orc.interactions_per_eval([1, 0, 0, 16, 0, 16367, 0]) == 17 * 16383 + 16367 * 17
+
+
+@pytest.mark.parametrize("name", ["initial_disk.npz", "initial_branches.npz"])
+def test_initial_generator_matches_red(name):
+    """oracle/red_initial.py against red.cuda.initial's own generator (golden
+    vectors from oracle/_ref/initial_harness): every drawn and derived
+    quantity bit for bit, positions and velocities to 1e-15 relative (numpy's
+    sin / cos / atan / tan against the C library's)."""
+    from oracle import red_initial
+    g = golden(name)
+    d, dt = red_initial.populate(bytes(g["spec"]).decode())
+    assert np.array_equal(d["oe"], g["oe"])
+    for f in ("mass", "radius", "density", "cd"):
+        assert np.array_equal(d[f], g["p"][f]), f
+    assert np.array_equal(d["id"], g["md"]["id"]) and np.array_equal(d["body_type"], g["md"]["body_type"])
+    for q in ("r", "v"):
+        ref = np.stack([g[q]["x"], g[q]["y"], g[q]["z"]], axis=1)
+        assert np.allclose(d[q], ref, rtol=1e-15, atol=1e-15 * np.abs(ref).max()), q
+    assert dt == pytest.approx(float(g["dt"]), rel=1e-15)
+
+
+def test_ic_draws_and_recipe_follow_red(rg):
+    """red.cuda_gb300/ic.py, the generator of the bench's disks, against the
+    pinned restatement: its random source gives red's draws bit for bit, and
+    its Kepler solver, element-to-Cartesian conversion and barycentre give the
+    same state from the same elements (the golden disk's)."""
+    from oracle import red_initial
+    s = rg.ic.RedStreams(7)
+    for k, (kind, args, n) in enumerate([("uniform", (0.7, 1.5), 500), ("rayleigh", (0.02,), 500),
+                                         ("power", (0.5, 3.0, -1.0), 300)]):
+        got = getattr(s, kind)(*args, n) if kind != "uniform" else s.uniform(*args, n)
+        ref = red_initial.Distribution(kind, 64 * 7 + k, *args).draw(n)
+        assert np.array_equal(got, ref), kind
+    s = rg.ic.RedStreams(11)
+    rr = red_initial.RedRandom(64 * 11)
+    assert s.integer(128, 4096) == 128 + int(rr.rand() / 4294967296. * (4096 - 128 + 1))
+    g = golden("initial_disk.npz")
+    d, _ = red_initial.populate(bytes(g["spec"]).decode())
+    oe, mass = d["oe"], d["mass"]
+    mu = rg.ic.K2 * (mass[0] + mass[1:])
+    r, v = rg.ic.calc_phase(mu, oe[1:, 0], oe[1:, 1], oe[1:, 2], oe[1:, 3], oe[1:, 4], oe[1:, 5])
+    rr_, vv_ = red_initial.calc_phase(mu, oe[1:, 0], oe[1:, 1], oe[1:, 2], oe[1:, 3], oe[1:, 4], oe[1:, 5])
+    assert np.array_equal(r, rr_) and np.array_equal(v, vv_)
+    R = np.zeros(len(mass), rg.types.VAR4)
+    V = np.zeros(len(mass), rg.types.VAR4)
+    for k, c in enumerate("xyz"):
+        R[c][1:], V[c][1:] = r[:, k], v[:, k]
+    rg.ic.to_barycentre(mass, R, V)
+    R2 = np.vstack([np.zeros(3), r])
+    V2 = np.vstack([np.zeros(3), v])
+    red_initial.transform_to_bc(mass, R2, V2, d["id"])
+    for k, c in enumerate("xyz"):
+        assert np.array_equal(R[c], R2[:, k]) and np.array_equal(V[c], V2[:, k])
