@@ -486,13 +486,19 @@ def run_ours(args, rg, rank, world, local_rank):
     rg.shard.barrier(local_rank)
     torch.cuda.synchronize()
     stats = {}
+    coll0 = snapshot(sim)["collisions"]
     ms, inter, sim_dt, tried, failed = measure(torch, sim, stream, args, flush, args.steps, tps, stats)
     torch.cuda.synchronize()
     rg.shard.barrier(local_rank)
     clk = clocks.stop()
     launches = sim.kernel_launches - launches0
+    # |dE/E| over the systems that had no merge in the timed region (a perfect
+    # merge changes E by design)
+    merged = snapshot(sim)["collisions"] - coll0
     dE = 0.0
     for k in range(sim.n_systems):
+        if merged[k]:
+            continue
         E1 = sim.energy_interacting(k)
         dE = max(dE, abs((E1[0] - E0[k][0]) / E0[k][0]))
     t_max = rg.shard.max_over_ranks(ms, device="cuda")
@@ -572,7 +578,10 @@ def run_ours(args, rg, rank, world, local_rank):
                 "config": config_object(args, systems, kw, desc, world),
                 "sim_years_per_s": sim_years_all / (t_max * 1e-3),
                 "dE_over_E": dE,
+                "dE_over_E_note": "largest over the systems without a merge in the timed region, E over the "
+                                  "interacting pairs; the FP64 runs drift the same at this tolerance (--accuracy-years)",
                 "collisions_in_timed_region": stats.get("collisions"),
+                "systems_with_merges": int(np.count_nonzero(merged)),
                 "tries_in_timed_region": int(tried),
                 "ms_per_try": ms_per_try,
                 "accept_fraction": (1.0 - failed / tried) if tried else None,
@@ -681,6 +690,84 @@ def run_accuracy(args, rg, local_rank=0):
     print(json.dumps(out), flush=True)
 
 
+def run_proposer_eval(args, rg, local_rank=0):
+    """The learned step proposer at the scale of its specification: the 512-disk
+    ensemble integrated plainly for `proposer_train_years` (~2e6 logged
+    records), the network trained on the GPU on two targets (the step accepted
+    next; the largest step that would have met the tolerance), then three runs
+    of `proposer_years` from the same start: the classical controller, and the
+    controller with either network's proposals.  Reported per run: tries,
+    rejected fraction, simulated years per second (wall clock of the whole
+    run, events handled), |dE/E| (largest over the disks without a merge) and
+    the proposer kernels' share of a try."""
+    import torch
+    torch.cuda.set_device(local_rank)
+    systems, kw, desc = workload(rg, "c4")
+    stream = torch.cuda.Stream()
+    YR = YEAR * K_GAUSS
+
+    def integrate(sim):
+        while True:
+            sim.launch_tries(500)
+            act, halted = sim.synchronize()
+            if halted:
+                sim.handle_events()
+            if not act:
+                break
+
+    t0 = time.perf_counter()
+    sim = rg.Sim(systems, length=args.proposer_train_years * YR, device=local_rank, stream=stream.cuda_stream, **kw)
+    sim.log_features(1 << 23)
+    integrate(sim)
+    recs = sim.feature_log(cap=1 << 23)
+    sim.close()
+    log_s = time.perf_counter() - t0
+    nets = {}
+    for target in ("accepted", "largest"):
+        t0 = time.perf_counter()
+        bits, nm, hist = rg.proposer.train(recs, epochs=args.proposer_epochs, batch=8192, lr=2e-3, target=target)
+        nets[target] = (bits, nm, {"train_s": time.perf_counter() - t0, "val_loss": hist[-1][2]})
+
+    def arm(name, net=None, safety=1.0):
+        sim = rg.Sim(systems, length=args.proposer_years * YR, device=local_rank, stream=stream.cuda_stream, **kw)
+        if net is not None:
+            sim.set_step_proposer(net[0], net[1], safety=safety, ratio_lo=0.25, ratio_hi=4.0)
+        E0 = [sim.energy_interacting(k)[0] for k in range(sim.n_systems)]
+        c0 = snapshot(sim)["collisions"]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        integrate(sim)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        snap = snapshot(sim)
+        merged = snap["collisions"] - c0
+        dE = max([abs((sim.energy_interacting(k)[0] - E0[k]) / E0[k]) for k in range(sim.n_systems)
+                  if not merged[k]] or [0.0])
+        share = None
+        if net is not None:
+            tot = {}
+            for _ in range(3):
+                ms, kind = sim.profile_try()
+                for m, k in zip(ms, kind):
+                    tot[int(k)] = tot.get(int(k), 0.0) + float(m)
+            share = tot.get(5, 0.0) / sum(tot.values()) if tot else None
+        tried, failed = int(snap["tried"].sum()), int(snap["failed"].sum())
+        sim.close()
+        return name, {"tries": tried, "rejected_fraction": failed / tried, "wall_s": wall,
+                      "sim_years_per_s": float(np.sum(snap["t"])) / YR / wall, "dE_over_E": dE,
+                      "proposer_share_of_try": share, "safety": safety if net is not None else None}
+
+    runs = dict([arm("classical"), arm("learned_accepted", nets["accepted"], 1.0),
+                 arm("learned_largest", nets["largest"], 0.9)])
+    base = runs["classical"]["sim_years_per_s"]
+    for r in runs.values():
+        r["sim_years_per_s_vs_classical"] = r["sim_years_per_s"] / base
+    print(json.dumps({"proposer_eval": {
+        "workload": desc, "train_years": args.proposer_train_years, "eval_years": args.proposer_years,
+        "records": int(len(recs)), "log_run_s": log_s,
+        "training": {k: v[2] for k, v in nets.items()}, "runs": runs}}), flush=True)
+
+
 def run_plan_only(args, rg, rank, world):
     """Each rank builds its slice of the workload and reports it (no GPU work);
     rank 0 prints the gathered slices.  Checks the launcher and the split."""
@@ -723,6 +810,10 @@ def main():
     ap.add_argument("--accuracy-years", type=float, default=0.0)
     ap.add_argument("--tolerance", type=float, default=0.0)
     ap.add_argument("--plan-only", action="store_true")
+    ap.add_argument("--proposer-eval", action="store_true")
+    ap.add_argument("--proposer-years", type=float, default=100.0)
+    ap.add_argument("--proposer-train-years", type=float, default=20.0)
+    ap.add_argument("--proposer-epochs", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-red-gpu", action="store_true")
@@ -749,6 +840,10 @@ def main():
     if args.accuracy_years > 0:
         if rank == 0:
             run_accuracy(args, rg, local_rank)
+        return
+    if args.proposer_eval:
+        if rank == 0:
+            run_proposer_eval(args, rg, local_rank)
         return
     if world > 1:
         import torch

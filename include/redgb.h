@@ -334,8 +334,9 @@ int red_mlp_adam(float* master, void* w_bf16, float* m, float* v, const float* g
 int red_set_step_proposer(red_sim* sim, const uint16_t* w_bf16, const red_mlp_norm_t* norm, double safety,
                           double ratio_lo, double ratio_hi);
 int red_clear_step_proposer(red_sim* sim);
-/* Logs (features of an accepted state, log|dt| of the next accepted step)
- * records, 13 floats each, into a device buffer of `capacity` records (0 stops). */
+/* Logs (features of an accepted state, log|dt| of the next accepted step,
+ * log(err / tol) of that step) records, 14 floats each, into a device buffer
+ * of `capacity` records (0 stops). */
 int red_log_features(red_sim* sim, uint32_t capacity);
 int red_get_feature_log(red_sim* sim, float* out, uint32_t cap, uint32_t* n_out, int32_t reset);
 

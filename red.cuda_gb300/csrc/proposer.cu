@@ -219,9 +219,10 @@ __global__ void k_propose(const ProposeParams P)
         if (P.has_prev[s]) {
             const unsigned k = atomicAdd(P.log_n, 1u);
             if (k < P.log_cap) {
-                float* r = P.log_buf + (size_t)k * (kFeat + 1);
+                float* r = P.log_buf + (size_t)k * kLogRec;
                 for (int c = 0; c < kFeat; c++) r[c] = P.feat_prev[s * kFeat + c];
-                r[kFeat] = f[0];   // log|dt| of the step accepted after those features
+                r[kFeat] = f[0];       // log|dt| of the step accepted after those features
+                r[kFeat + 1] = f[1];   // log(err / tol) of that step
             }
         }
         for (int c = 0; c < kFeat; c++) P.feat_prev[s * kFeat + c] = f[c];

@@ -7,6 +7,7 @@
 namespace redgb {
 
 constexpr int kFeat = 12;      // features per system
+constexpr int kLogRec = kFeat + 2;   // floats per logged record: features, log|dt|, log(err / tol)
 constexpr int kHid = 64;       // hidden width of both layers
 // parameters, flat: W1[kHid][kFeat], b1[kHid], W2[kHid][kHid], b2[kHid], w3[kHid], b3
 constexpr int oW1 = 0;

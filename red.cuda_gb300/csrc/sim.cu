@@ -2254,7 +2254,7 @@ int red_log_features(red_sim* sim, uint32_t capacity)
     sim->log_cap = 0;
     sim->log_on = capacity > 0;
     if (sim->log_on) {
-        sim->d_log = dalloc<float>((size_t)capacity * (kFeat + 1));
+        sim->d_log = dalloc<float>((size_t)capacity * kLogRec);
         sim->log_cap = capacity;
         if (!sim->d_log_n) sim->d_log_n = dalloc<unsigned int>(1);
         if (!sim->d_feat_prev) {
@@ -2281,7 +2281,7 @@ int red_get_feature_log(red_sim* sim, float* out, uint32_t cap, uint32_t* n_out,
     const uint32_t n = std::min<uint32_t>(count, sim->log_cap);
     *n_out = n;
     const uint32_t k = std::min(n, cap);
-    if (k) CK(cudaMemcpy(out, sim->d_log, (size_t)k * (kFeat + 1) * sizeof(float), cudaMemcpyDeviceToHost));
+    if (k) CK(cudaMemcpy(out, sim->d_log, (size_t)k * kLogRec * sizeof(float), cudaMemcpyDeviceToHost));
     if (reset && sim->d_log_n) CK(cudaMemset(sim->d_log_n, 0, sizeof(unsigned int)));
     return RED_OK;
     GUARD_END

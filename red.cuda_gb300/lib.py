@@ -436,8 +436,9 @@ class Sim:
         _check(load().red_log_features(self.h, capacity))
 
     def feature_log(self, cap=1 << 20, reset=False):
-        """Logged records as an (n, 13) float32 array: 12 features, log|dt| of the next accepted step."""
-        out = np.zeros((cap, MLP_NFEAT + 1), np.float32)
+        """Logged records as an (n, 14) float32 array: 12 features, log|dt| of the
+        next accepted step, log(err / tol) of that step."""
+        out = np.zeros((cap, MLP_NFEAT + 2), np.float32)
         n = C.c_uint32()
         _check(load().red_get_feature_log(self.h, _p(out), cap, C.byref(n), 1 if reset else 0))
         return out[:min(n.value, cap)].copy()

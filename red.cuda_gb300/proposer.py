@@ -2,8 +2,8 @@
 
 The network (12 -> 64 -> 64 -> 1, SiLU, BF16 weights, FP32 accumulation) and
 its forward, backward and Adam kernels live in libredgb (proposer.cu); this
-module only moves the data: it standardises the logged (features, log|dt|)
-records, keeps the parameters, the Adam moments and the batches in device
+module only moves the data: it standardises the logged (features, log|dt|,
+log(err / tol)) records, keeps the parameters, the Adam moments and the batches in device
 memory (torch tensors as plain buffers) and calls red_mlp_grad /
 red_mlp_adam for every batch.  Records come from Sim.log_features /
 Sim.feature_log on plain runs of the integrator.
@@ -40,10 +40,26 @@ def init_params(seed=0):
     return p
 
 
-def make_norm(records):
-    """red_mlp_norm_t from logged records (n, 13)."""
-    x = records[:, :NFEAT].astype(np.float64)
+def records_xt(records, target="accepted", order=7):
+    """Inputs and targets of logged records (n, 14): the 12 features and either
+    the log|dt| of the step accepted next ("accepted": the network imitates
+    the classical controller's outcome) or the log of the largest step that
+    would have met the tolerance there ("largest": log|dt| - log(err/tol) / order,
+    the correction clipped to a factor 4 either way), so that safety * exp(y)
+    aims just inside the tolerance."""
+    x = records[:, :NFEAT]
     t = records[:, NFEAT].astype(np.float64)
+    if target == "largest":
+        t = t + np.clip(-records[:, NFEAT + 1].astype(np.float64) / order, -np.log(4.0), np.log(4.0))
+    elif target != "accepted":
+        raise ValueError("unknown target " + target)
+    return x, t
+
+
+def make_norm(x, t):
+    """red_mlp_norm_t from features x (n, 12) and targets t (n,)."""
+    x = np.asarray(x, np.float64)
+    t = np.asarray(t, np.float64)
     nm = lib.MlpNorm()
     mu = x.mean(axis=0)
     sd = np.maximum(x.std(axis=0), 1e-3)
@@ -55,15 +71,16 @@ def make_norm(records):
     return nm
 
 
-def normalise(records, nm):
-    x = (records[:, :NFEAT] - np.array(nm.x_mean, np.float32)) / np.array(nm.x_std, np.float32)
-    t = (records[:, NFEAT] - np.float32(nm.y_mean)) / np.float32(nm.y_std)
+def normalise(x, t, nm):
+    x = (np.asarray(x, np.float32) - np.array(nm.x_mean, np.float32)) / np.array(nm.x_std, np.float32)
+    t = (np.asarray(t, np.float32) - np.float32(nm.y_mean)) / np.float32(nm.y_std)
     return np.ascontiguousarray(x, np.float32), np.ascontiguousarray(t, np.float32)
 
 
-def train(records, epochs=30, batch=2048, lr=2e-3, seed=0, val_frac=0.1, device="cuda"):
+def train(records, epochs=30, batch=2048, lr=2e-3, seed=0, val_frac=0.1, device="cuda", target="accepted",
+          order=7):
     """Trains on the GPU; returns (BF16 weights as uint16, MlpNorm, history of
-    (epoch, train loss, validation loss))."""
+    (epoch, train loss, validation loss)).  `target`: see records_xt."""
     import torch
     records = np.asarray(records, np.float32)
     records = records[np.isfinite(records).all(axis=1)]
@@ -76,9 +93,9 @@ def train(records, epochs=30, batch=2048, lr=2e-3, seed=0, val_frac=0.1, device=
     perm = rng.permutation(len(records))
     n_val = max(16, int(val_frac * len(records)))
     val, tr = records[perm[:n_val]], records[perm[n_val:]]
-    nm = make_norm(tr)
-    xtr, ttr = normalise(tr, nm)
-    xval, tval = normalise(val, nm)
+    nm = make_norm(*records_xt(tr, target, order))
+    xtr, ttr = normalise(*records_xt(tr, target, order), nm)
+    xval, tval = normalise(*records_xt(val, target, order), nm)
     dev = torch.device(device)
     X = torch.from_numpy(xtr).to(dev)
     T = torch.from_numpy(ttr).to(dev)

@@ -134,6 +134,7 @@ def test_features_match_the_state(rg):
     assert np.allclose(f[keep], ref[keep], rtol=2e-4, atol=2e-5), (f[keep], ref[keep])
     assert f[1] <= 0.0                              # the accepted step's error was within tolerance
     assert f[12] == pytest.approx(np.log(abs(dt2)), rel=1e-6)
+    assert f[13] <= 0.0                             # log(err / tol) of the second accepted step
 
 
 def test_trained_proposer_reduces_rejected_tries(rg):
