@@ -208,6 +208,7 @@ typedef struct {
     int32_t chunk;                /* sources per chunk (0: the planner's heuristic) */
     int32_t lanes_cap;            /* largest threads per sink group */
     int32_t cluster;              /* chunk sums reduced within thread-block clusters */
+    int32_t packed;               /* 2-sink tiles on the packed FP32-pair instance */
     int32_t n_items;              /* stage-kernel CTAs of one launch */
     int32_t candidates;           /* plans timed by the last red_autotune (0: none) */
     float ms_per_try;             /* its best try time */

@@ -165,6 +165,7 @@ struct StageParams {
     long long head_n;
     int cluster;          // 1: launched in clusters of kClusterChunks CTAs (items laid out for it)
     int one_wave;         // 1: the launch is one wave (one kernel instance for every variant)
+    int packed;           // 1: plans of many waves with 2-sink tiles take the packed-pair instance
 };
 
 struct FinishParams {

@@ -440,6 +440,8 @@ struct red_sim {
     bool use_cluster = false;   // the plan's items are laid out for a cluster launch
     int lanes_cap = 32;         // upper bound on threads per sink (autotuner)
     bool allow_cluster = true;  // the planner may lay chunk groups out as clusters (autotuner)
+    bool allow_packed = true;   // plans of 2-sink tiles may take the packed-pair instance (autotuner)
+    bool use_packed = false;    // the plan's stage launches take the packed-pair instance
     red_plan_info_t plan_info{};   // what the last red_autotune measured
 
     cudaGraphExec_t graph = nullptr;
@@ -776,6 +778,17 @@ void red_sim::build_plan()
             }
         }
     }
+    // A plan of many waves whose tiles mostly hold 2 sinks per thread (FP32
+    // modes) takes the packed-pair stage instance.
+    // REDGB_PACKED=0 keeps the scalar instance.
+    use_packed = false;
+    const char* penv = getenv("REDGB_PACKED");
+    if ((mode == MODE_MIXED || mode == MODE_FP32) && allow_packed && !(penv && penv[0] == '0') && !use_cluster &&
+        items.size() > (size_t)6 * 152) {
+        size_t n2 = 0;
+        for (const GravItem& g : items) n2 += g.spt == 2 ? 1 : 0;
+        use_packed = 2 * n2 >= items.size();
+    }
     auto upload = [&](auto& vec, auto*& dptr, size_t& cap) {
         using T = typename std::remove_reference<decltype(vec)>::type::value_type;
         if (vec.size() > cap) {
@@ -868,6 +881,7 @@ StageParams red_sim::stage_params(int s, bool standalone)
     P.tile_cnt = tile_cnt;
     P.cluster = use_cluster ? 1 : 0;
     P.one_wave = items.size() <= (size_t)6 * 152 ? 1 : 0;
+    P.packed = use_packed ? 1 : 0;
     P.gas.enabled = cfg.gas_disk == 1;
     for (int k = 0; k < 2; k++) {
         P.gas.rho[k] = cfg.gas.rho[k];
@@ -2099,6 +2113,7 @@ int red_autotune(red_sim* sim)
         info.chunk = sim->chunk_override;
         info.lanes_cap = sim->lanes_cap;
         info.cluster = sim->use_cluster ? 1 : 0;
+        info.packed = sim->use_packed ? 1 : 0;
         info.n_items = (int32_t)sim->items.size();
         return RED_OK;
     }
@@ -2132,12 +2147,14 @@ int red_autotune(red_sim* sim)
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    struct Cand { int chunk, lanes; bool cluster; };
+    struct Cand { int chunk, lanes; bool cluster, packed; };
     std::vector<Cand> cands;
     for (int lanes : {32, 16, 8}) {
-        cands.push_back({0, lanes, true});
-        cands.push_back({0, lanes, false});
-        for (int c : {256, 512, 1024, 2048}) cands.push_back({c, lanes, false});
+        cands.push_back({0, lanes, true, true});
+        for (bool pk : {true, false}) {
+            cands.push_back({0, lanes, false, pk});
+            for (int c : {256, 512, 1024, 2048}) cands.push_back({c, lanes, false, pk});
+        }
     }
     float best = 1e30f;
     Cand best_c = cands[0];
@@ -2146,8 +2163,10 @@ int red_autotune(red_sim* sim)
         sim->chunk_override = c.chunk;
         sim->lanes_cap = c.lanes;
         sim->allow_cluster = c.cluster;
+        sim->allow_packed = c.packed;
         sim->build_plan();
-        if (c.cluster && !sim->use_cluster && c.chunk == 0) continue;   // same plan as the next candidate
+        if (c.cluster && !sim->use_cluster && c.chunk == 0) continue;   // same plan as a later candidate
+        if (c.packed && !sim->use_packed) continue;                       // the same as its unpacked twin
         sim->prep_positions();
         sim->launch_tries(2);                  // graph capture, warm caches
         if (reps == 0) {
@@ -2179,6 +2198,7 @@ int red_autotune(red_sim* sim)
     sim->chunk_override = best_c.chunk;
     sim->lanes_cap = best_c.lanes;
     sim->allow_cluster = best_c.cluster;
+    sim->allow_packed = best_c.packed;
     sim->build_plan();
     swap_state(false);
     sim->ejhc_initial_done = ejhc_done;
@@ -2189,6 +2209,7 @@ int red_autotune(red_sim* sim)
     info.chunk = sim->chunk_override;
     info.lanes_cap = sim->lanes_cap;
     info.cluster = sim->use_cluster ? 1 : 0;
+    info.packed = sim->use_packed ? 1 : 0;
     info.n_items = (int32_t)sim->items.size();
     info.ms_per_try = best;
     return RED_OK;
@@ -2203,6 +2224,7 @@ int red_get_plan_info(red_sim* sim, red_plan_info_t* out)
     i.chunk = sim->chunk_override;
     i.lanes_cap = sim->lanes_cap;
     i.cluster = sim->use_cluster ? 1 : 0;
+    i.packed = sim->use_packed ? 1 : 0;
     i.n_items = (int32_t)sim->items.size();
     *out = i;
     return RED_OK;

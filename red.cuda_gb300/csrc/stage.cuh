@@ -291,6 +291,162 @@ __device__ __forceinline__ void gravity_f32(SmemStage& sm, const StageParams& P,
     mine_ok = lane < 3 * SPT && mine_k < it.nsink;
 }
 
+// The same gravity for tiles of 2 sinks per thread on 8 lanes, with packed
+// FP32 pairs (add / mul / fma .f32x2: one instruction for two interactions).
+// The lanes step over pairs of sources.  Each tile, staged in shared memory
+// as one float4 per source, is first rewritten in place as pair records:
+//   A[p] = (x_2p, x_2p+1, y_2p, y_2p+1), B[p] = (z_2p, z_2p+1, m_2p, m_2p+1)
+// and, for the double-single low parts, C[p] = (x, x', y, y') and D[p] = (z, z').
+// An odd source count pads the last pair with a copy of its first source of
+// mass 0 (its term is 0 * finite).  The sums are those of gravity_f32 in
+// another grouping: each lane's tile sum is the sum of its two pair halves.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+template <int MODE>
+__device__ __forceinline__ void pair_tiles(SmemStage& sm, int nsrc, int ntile)
+{
+    // tile tau (kTile sources at tau * kTile) -> its pair records, in place
+    const int t = threadIdx.x;
+    constexpr int kHalf = kTile / 2;
+    const int tau = t / kHalf, lp = t % kHalf;
+    const int b = tau * kTile;
+    const int nt = min(kTile, nsrc - tau * kTile);
+    const bool on = tau < ntile && 2 * lp < nt;
+    float4 h0 = make_float4(0.f, 0.f, 0.f, 0.f), h1 = h0, l0 = h0, l1 = h0;
+    if (on) {
+        h0 = sm.src.f.hi[b + 2 * lp];
+        if (MODE == MODE_MIXED) l0 = sm.src.f.lo[b + 2 * lp];
+        if (2 * lp + 1 < nt) {
+            h1 = sm.src.f.hi[b + 2 * lp + 1];
+            if (MODE == MODE_MIXED) l1 = sm.src.f.lo[b + 2 * lp + 1];
+        } else {
+            h1 = make_float4(h0.x, h0.y, h0.z, 0.f);
+            l1 = l0;
+        }
+    }
+    __syncthreads();
+    if (on) {
+        sm.src.f.hi[b + lp] = make_float4(h0.x, h1.x, h0.y, h1.y);
+        sm.src.f.hi[b + kHalf + lp] = make_float4(h0.z, h1.z, h0.w, h1.w);
+        if (MODE == MODE_MIXED) {
+            sm.src.f.lo[b + lp] = make_float4(l0.x, l1.x, l0.y, l1.y);
+            sm.src.f.lo[b + kHalf + lp] = make_float4(l0.z, l1.z, 0.f, 0.f);
+        }
+    }
+    __syncthreads();
+}
+
+template <int MODE>
+__device__ __forceinline__ void gravity_f32_pair(SmemStage& sm, const StageParams& P, const GravItem& it,
+                                                 bool staged, float4& th, float4& tl, float2& mine, int& mine_k,
+                                                 bool& mine_ok)
+{
+    constexpr int SPT = 2, L = 8, kHalf = kTile / 2;
+    const int t = threadIdx.x;
+    const int grp = t / L, lane = t % L;
+    float2 nHx[SPT], nHy[SPT], nHz[SPT], nLx[SPT], nLy[SPT], nLz[SPT];
+#pragma unroll
+    for (int q = 0; q < SPT; q++) {
+        const int k = grp * SPT + q;
+        const int ks = k < it.nsink ? k : 0;   // inactive slots shadow sink 0 (results unused)
+        const float4 H = sm.snk.f.hi[ks];
+        const float4 Lo = MODE == MODE_MIXED ? sm.snk.f.lo[ks] : make_float4(0.f, 0.f, 0.f, 0.f);
+        nHx[q] = f2(-H.x, -H.x);
+        nHy[q] = f2(-H.y, -H.y);
+        nHz[q] = f2(-H.z, -H.z);
+        nLx[q] = f2(-Lo.x, -Lo.x);
+        nLy[q] = f2(-Lo.y, -Lo.y);
+        nLz[q] = f2(-Lo.z, -Lo.z);
+    }
+    float acc[SPT][6];
+#pragma unroll
+    for (int q = 0; q < SPT; q++)
+#pragma unroll
+        for (int c = 0; c < 6; c++) acc[q][c] = 0.f;
+    if (staged) pair_tiles<MODE>(sm, it.src1 - it.src0, (it.src1 - it.src0 + kTile - 1) / kTile);
+    for (int j0 = it.src0; j0 < it.src1; j0 += kTile) {
+        const int nj = min(kTile, it.src1 - j0);
+        const bool more = !staged && j0 + kTile < it.src1;
+        const int base = staged ? j0 - it.src0 : 0;   // staged chunks hold all their tiles
+        if (more && t < min(kTile, it.src1 - j0 - kTile)) {
+            th = P.pos_hi_in[j0 + kTile + t];
+            if (MODE == MODE_MIXED) tl = P.pos_lo_in[j0 + kTile + t];
+        }
+        if (!staged) pair_tiles<MODE>(sm, nj, 1);
+        const float4* A = sm.src.f.hi + base;
+        const float4* B = A + kHalf;
+        const float4* Cl = sm.src.f.lo + base;
+        const float4* Dl = Cl + kHalf;
+        float2 tx[SPT], ty[SPT], tz[SPT];
+#pragma unroll
+        for (int q = 0; q < SPT; q++) tx[q] = ty[q] = tz[q] = f2(0.f, 0.f);
+        const int np = (nj + 1) >> 1;
+        const float2 eps2 = f2(kEps2, kEps2);
+#pragma unroll 4
+        for (int pp = lane; pp < np; pp += L) {
+            const float4 a = A[pp], bz = B[pp];
+            float4 c = make_float4(0.f, 0.f, 0.f, 0.f), d = c;
+            if (MODE == MODE_MIXED) {
+                c = Cl[pp];
+                d = Dl[pp];
+            }
+#pragma unroll
+            for (int q = 0; q < SPT; q++) {
+                float2 dx = __fadd2_rn(f2(a.x, a.y), nHx[q]);
+                float2 dy = __fadd2_rn(f2(a.z, a.w), nHy[q]);
+                float2 dz = __fadd2_rn(f2(bz.x, bz.y), nHz[q]);
+                if (MODE == MODE_MIXED) {
+                    dx = __fadd2_rn(dx, __fadd2_rn(f2(c.x, c.y), nLx[q]));
+                    dy = __fadd2_rn(dy, __fadd2_rn(f2(c.z, c.w), nLy[q]));
+                    dz = __fadd2_rn(dz, __fadd2_rn(f2(d.x, d.y), nLz[q]));
+                }
+                float2 r2 = __ffma2_rn(dx, dx, eps2);
+                r2 = __ffma2_rn(dy, dy, r2);
+                r2 = __ffma2_rn(dz, dz, r2);
+                const float2 ri = f2(rsqrtf(r2.x), rsqrtf(r2.y));
+                const float2 sc = __fmul2_rn(__fmul2_rn(f2(bz.z, bz.w), ri), __fmul2_rn(ri, ri));
+                tx[q] = __ffma2_rn(sc, dx, tx[q]);
+                ty[q] = __ffma2_rn(sc, dy, ty[q]);
+                tz[q] = __ffma2_rn(sc, dz, tz[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < SPT; q++) {
+            ds_add(acc[q][0], acc[q][1], tx[q].x + tx[q].y);
+            ds_add(acc[q][2], acc[q][3], ty[q].x + ty[q].y);
+            ds_add(acc[q][4], acc[q][5], tz[q].x + tz[q].y);
+        }
+        if (more) {
+            __syncthreads();
+            sm.src.f.hi[t] = th;
+            if (MODE == MODE_MIXED) sm.src.f.lo[t] = tl;
+            __syncthreads();
+        }
+    }
+    for (int o = 1; o < L; o <<= 1) {
+#pragma unroll
+        for (int q = 0; q < SPT; q++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const float oh = __shfl_xor_sync(0xffffffffu, acc[q][2 * c], o);
+                const float ol = __shfl_xor_sync(0xffffffffu, acc[q][2 * c + 1], o);
+                ds_merge(acc[q][2 * c], acc[q][2 * c + 1], oh, ol);
+            }
+    }
+    float hh = 0.f, ll = 0.f;
+#pragma unroll
+    for (int q = 0; q < SPT; q++)
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            if (lane == 3 * q + c) {
+                hh = acc[q][2 * c];
+                ll = acc[q][2 * c + 1];
+            }
+    mine = dsn_norm(hh, ll);
+    mine_k = grp * SPT + lane / 3;
+    mine_ok = lane < 3 * SPT && mine_k < it.nsink;
+}
+
 // Gravity of the chunk's sources, FP64 modes (one sink per thread group).
 template <int MODE>
 __device__ __forceinline__ void gravity_f64(SmemStage& sm, const StageParams& P, const GravItem& it, D4& td, int& tid,
@@ -395,8 +551,8 @@ __device__ __forceinline__ void gravity_f64(SmemStage& sm, const StageParams& P,
 // CTA hides more of it (512-disk ensemble stage -17 %, 65536-body gas-drag
 // disk -13 %, all-pairs 16384-body disk -1.3 %; 8 CTAs at 64 registers spill
 // and are slower).  The one-wave instance keeps 80 registers.
-template <int MODE, bool EXACT, bool CL, int VT>
-__global__ void __launch_bounds__(kTile, VT >= 0 ? 7 : 6) k_stage(const StageParams P, const int Vrt)
+template <int MODE, bool EXACT, bool CL, int VT, bool PK = false>
+__global__ void __launch_bounds__(kTile, PK ? 6 : (VT >= 0 ? 7 : 6)) k_stage(const StageParams P, const int Vrt)
 {
     constexpr bool kF32 = (MODE == MODE_MIXED || MODE == MODE_FP32);
     const int V = VT >= 0 ? VT : Vrt;
@@ -568,7 +724,8 @@ __global__ void __launch_bounds__(kTile, VT >= 0 ? 7 : 6) k_stage(const StagePar
     int mine_k;
     bool mine_ok;
     if constexpr (kF32) {
-        if (it.spt == 2) gravity_f32<MODE, 2>(sm, P, it, staged, th, tl, mine_ds, mine_k, mine_ok);
+        if (PK && it.spt == 2) gravity_f32_pair<MODE>(sm, P, it, staged, th, tl, mine_ds, mine_k, mine_ok);
+        else if (!PK && it.spt == 2) gravity_f32<MODE, 2>(sm, P, it, staged, th, tl, mine_ds, mine_k, mine_ok);
         else gravity_f32<MODE, 1>(sm, P, it, staged, th, tl, mine_ds, mine_k, mine_ok);
     } else {
         gravity_f64<MODE>(sm, P, it, td, tid, mine, mine_k, mine_ok);
@@ -780,6 +937,14 @@ void stage_attributes()
 template <int MODE, bool EXACT, int VT>
 void launch_fixed(const StageParams& P, int n, int v, cudaStream_t s)
 {
+    // plans of 2-sink tiles on 8 lanes (P.packed, FP32 modes): the packed-pair
+    // instance, 6 CTAs per SM (its pair loop needs the registers of the seventh)
+    if constexpr (MODE == MODE_MIXED || MODE == MODE_FP32) {
+        if (P.packed) {
+            launch_k(k_stage<MODE, EXACT, false, VT, true>, (unsigned)n, (unsigned)kTile, s, P, v);
+            return;
+        }
+    }
     launch_k(k_stage<MODE, EXACT, false, VT>, (unsigned)n, (unsigned)kTile, s, P, v);
 }
 

@@ -77,7 +77,8 @@ NOALLOC_MAX_BODIES = 32768
 
 class PlanInfo(C.Structure):
     """red_plan_info_t: the launch plan in use and the last autotune's timings."""
-    _fields_ = [("chunk", C.c_int32), ("lanes_cap", C.c_int32), ("cluster", C.c_int32), ("n_items", C.c_int32),
+    _fields_ = [("chunk", C.c_int32), ("lanes_cap", C.c_int32), ("cluster", C.c_int32), ("packed", C.c_int32),
+                ("n_items", C.c_int32),
                 ("candidates", C.c_int32), ("ms_per_try", C.c_float), ("ms_per_try_default", C.c_float)]
 
 
@@ -418,7 +419,8 @@ class Sim:
     def plan_info(self):
         i = PlanInfo()
         _check(load().red_get_plan_info(self.h, C.byref(i)))
-        return {"chunk": i.chunk, "lanes_cap": i.lanes_cap, "cluster": bool(i.cluster), "n_items": i.n_items,
+        return {"chunk": i.chunk, "lanes_cap": i.lanes_cap, "cluster": bool(i.cluster), "packed": bool(i.packed),
+                "n_items": i.n_items,
                 "candidates": i.candidates, "ms_per_try": i.ms_per_try,
                 "ms_per_try_default": i.ms_per_try_default}
 

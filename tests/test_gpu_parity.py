@@ -442,3 +442,28 @@ def test_state_transfer_pinned_equals_pageable(rg):
             ends.append(sim.get_state(0))
     for f in ("r", "v", "p"):
         assert getattr(ends[0], f).tobytes() == getattr(ends[1], f).tobytes(), f
+
+
+@pytest.mark.parametrize("precision,bound", [("mixed", 1e-8), ("fp32", 5e-7)])
+def test_gravity_packed_pairs(rg, orc, monkeypatch, precision, bound):
+    """Plans of many waves whose tiles hold 2 sinks per thread take the packed
+    FP32-pair instance (sources in pairs, add / mul / fma .f32x2).  An all-SI
+    disk of 6017 bodies (source chunks of odd length, so the last pair of a
+    tile is padded) against the FP64 oracle with the all-SI tolerances (2e-6
+    for the star, FP32 pairs only; `bound` for the rest), and against the
+    scalar instance (REDGB_PACKED=0) to the same bound."""
+    s = rg.ic.config2(seed=44, n_pp=16, n_pl=6000).relabel_all_SI()
+    out = {}
+    for packed in ("1", "0"):
+        monkeypatch.setenv("REDGB_PACKED", packed)
+        with rg.Sim(s, dt=0.01, precision=precision) as sim:
+            out[packed] = (vec(sim.calc_dydx(0, 1, 0.0)), sim.plan_info())
+    assert out["1"][1]["packed"] and not out["0"][1]["packed"]
+    _, ref = orc.grav_accel(obody(orc, s), sem=orc.SEM_GPU, nthreads=16)
+    ref = vec(ref)
+    for packed in ("1", "0"):
+        a = out[packed][0]
+        err = np.linalg.norm(a - ref, axis=1) / np.linalg.norm(ref, axis=1)
+        assert err[0] < 2e-6 and err[1:].max() < bound, (packed, err[0], err[1:].max())
+    d = np.linalg.norm(out["1"][0] - out["0"][0], axis=1) / np.linalg.norm(ref, axis=1)
+    assert d[1:].max() < bound
