@@ -14,8 +14,12 @@ allocating side keeps the global chunk reduction, REDGB_CLUSTER=0, as the
 allocation-free entry point does), so the results agree to 1e-12 relative
 (they are expected to be identical).  At the largest accepted size, a dense
 system whose chunked plan would overflow the scratch array, the entry point
-sums each sink's sources in one CTA instead of in chunks, which reorders the
-double-single accumulation: 1e-10 relative there.
+sums each sink's sources in one CTA instead of in chunks.  That regroups the
+pair terms into other FP32 tile partials before their double-single sum, so
+the plans agree to MIXED's stated tolerances there: 2e-6 for the star, whose
+acceleration is a sum of FP32 pair terms only (the disk's pulls on it
+largely cancel), and 1e-10 for the bodies whose double-single star term
+dominates.
 
 A live simulation must not notice the entry point: a Sim stepped across a
 call follows the same trajectory, bit for bit, as one that never saw it.
@@ -149,7 +153,8 @@ def test_noalloc_largest_dense_system(rg):
         torch.cuda.synchronize()
         got = keep["accel"].cpu().numpy().reshape(-1, 3)
         err = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
-        assert err.max() <= 1e-10, err.max()
+        assert err[0] <= 2e-6, err[0]
+        assert err[1:].max() <= 1e-10, err[1:].max()
 
 
 def test_noalloc_restores_current_device(rg):
