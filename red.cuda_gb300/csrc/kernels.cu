@@ -10,6 +10,7 @@
 //   k_collision, k_grid_insert, k_grid_query   the same, for the explicit check
 //   k_ejhc      ejection / hit-centrum test
 //   k_potential per-body potential sums for the integrals
+#include <algorithm>
 #include <cfloat>
 #include <cstdio>
 
@@ -521,12 +522,26 @@ __global__ void k_set_quota(DevSys* sys, int n_sys, int q)
     if (s < n_sys) sys[s].quota = q;
 }
 
+// Empties the partial-record slots of the stage kernel's chunk reduction.
+__global__ void k_fill_records(unsigned long long* recs, size_t n)
+{
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        recs[k] = kRecEmpty;
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 void launch_set_quota(DevSys* sys, int n_sys, int q, cudaStream_t s)
 {
     if (n_sys > 0) k_set_quota<<<(unsigned)((n_sys + 127) / 128), 128, 0, s>>>(sys, n_sys, q);
+}
+
+void fill_records_empty(void* recs, size_t n, cudaStream_t s)
+{
+    if (n == 0) return;
+    const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 4 * 152);
+    k_fill_records<<<blocks, 256, 0, s>>>(static_cast<unsigned long long*>(recs), n);
 }
 
 void set_tableau(const Tableau& tb, cudaStream_t s)

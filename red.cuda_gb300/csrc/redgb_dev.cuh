@@ -241,9 +241,15 @@ struct EjhcParams {
     unsigned int capacity;
 };
 
+constexpr int kBatchRecords = 16;   // partial records loaded per batch by the reducing CTA
+// An empty partial-record slot (8 bytes) of the one-wave stage instance: a
+// signalling-NaN pattern no arithmetic produces.  Slots are filled with it
+// when a plan is built (fill_records_empty) and reset to it by the CTA that
+// sums them.
+constexpr unsigned long long kRecEmpty = 0x7ff0000000000001ull;
+
 // Host-side plan of the stage kernel for one system (sim.cu).
 // tiles_all: sink tiles of every system planned into the same launch (count_sink_tiles).
-constexpr int kBatchRecords = 16;   // partial records loaded per batch by the reducing CTA
 // short_ctas (optional) accumulates the CTAs the system would need with chunks of
 // two source tiles; short_chunks selects those chunks for the plan.
 int count_sink_tiles(const SysInfo& si, int mode, int lanes_cap, long long* short_ctas);
@@ -288,6 +294,8 @@ void launch_collision(const CollParams& P, int n_items, int n_segs, bool use_gri
 void launch_collide(const CollParams& P, int n_items, int n_segs, bool use_grid, cudaStream_t s);
 void launch_ejhc(const EjhcParams& P, int n_segs, cudaStream_t s);
 void launch_set_quota(DevSys* sys, int n_sys, int q, cudaStream_t s);
+// Sets n partial-record slots (8 bytes each) to kRecEmpty.
+void fill_records_empty(void* recs, size_t n, cudaStream_t s);
 // The three record arrays of red_get_state / red_set_state (r, v, p: 4 doubles
 // per body each).  Each is the device staging buffer or, when the caller's
 // array is pinned host memory, that array itself, read or written by the

@@ -836,6 +836,9 @@ void red_sim::build_plan()
         partial_cap = part;
         partial = dalloc<double>(3 * part);
     }
+    // The one-wave stage instance polls its partial records and needs their
+    // slots empty; the many-wave instances leave theirs filled.
+    fill_records_empty(partial, 3 * part, stream);
     if ((size_t)tiles > tile_cap) {
         cudaFree(tile_cnt);
         tile_cap = tiles;
@@ -2153,7 +2156,7 @@ int red_autotune(red_sim* sim)
         cands.push_back({0, lanes, true, true});
         for (bool pk : {true, false}) {
             cands.push_back({0, lanes, false, pk});
-            for (int c : {256, 512, 1024, 2048}) cands.push_back({c, lanes, false, pk});
+            for (int c : {256, 512, 1024, 2048, 4096}) cands.push_back({c, lanes, false, pk});
         }
     }
     float best = 1e30f;

@@ -101,6 +101,91 @@ __device__ __forceinline__ double sum_records(const double* base, long long stri
     return a;
 }
 
+// Polled partial records (the one-wave stage instance).  There the chunks of
+// a tile store their records and advance the tile's counter with no fence, so
+// each record carries its own readiness: its slot holds kRecEmpty
+// (redgb_dev.cuh), a signalling-NaN bit pattern that no arithmetic produces
+// (FP64 results carry the canonical quiet NaN; as a float2 it is a denormal
+// beside a non-canonical NaN), until its chunk's store lands.  The CTA that
+// takes the last count re-reads a record it finds empty, and resets every
+// slot it read to kRecEmpty for the next launch.  Every store it waits for has
+// been issued (the chunk's CTA passed a barrier after its stores, then
+// counted), so the wait ends within the memory system's latency; it is bounded
+// all the same: after kRecPollLimit reads a record counts as NaN and the
+// system's status is set to RED_ERR_TIMEOUT.  (The many-wave instances keep a
+// release fence before the count and an acquire fence after the last one, and
+// plain records: the fences' latency hides behind other CTAs there, and their
+// reducing CTAs would otherwise meet stores in flight.)
+constexpr unsigned long long kRecNaN = 0x7ff800007fc00000ull;   // NaN as a double and in both float halves
+constexpr int kRecPollLimit = 1 << 20;
+
+__device__ __forceinline__ void st_rec(unsigned long long* p, unsigned long long v)
+{
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;\n" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_rec(const unsigned long long* p)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];\n" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long rec_bits(float2 v)
+{
+    return ((unsigned long long)__float_as_uint(v.y) << 32) | __float_as_uint(v.x);
+}
+__device__ __forceinline__ unsigned long long rec_bits(double v) { return (unsigned long long)__double_as_longlong(v); }
+__device__ __forceinline__ void rec_add(float2& a, unsigned long long b)
+{
+    a = dsn_add(a, make_float2(__uint_as_float((unsigned)b), __uint_as_float((unsigned)(b >> 32))));
+}
+__device__ __forceinline__ void rec_add(double& a, unsigned long long b) { a += __longlong_as_double((long long)b); }
+
+// Re-reads the records [b, b1) until every chunk's store has landed (at most
+// kRecPollLimit reads each).  Returns false if one never does.
+__device__ __forceinline__ bool poll_records(const unsigned long long* base, long long stride, int b, int b1)
+{
+    bool ok = true;
+    for (int c = b; c < b1; c++) {
+        unsigned long long v = kRecEmpty;
+        for (int n = 0; v == kRecEmpty && n < kRecPollLimit; n++) v = ld_rec(base + c * stride);
+        ok = ok && v != kRecEmpty;
+    }
+    return ok;
+}
+
+// Sum of the polled records [c0, c1) of one element (element t of the tile at
+// offset t, `stride` words per chunk), in chunk order: double-single for the
+// float2 records of the FP32 modes, FP64 otherwise.  Loads are issued in
+// batches of kBatchRecords; a batch with a record still empty waits for its
+// records (poll_records) and is read again.  The slots are then emptied.
+// Returns false if a record stayed empty (it then adds NaN).
+template <typename T>
+__device__ __forceinline__ bool sum_polled_records(unsigned long long* base, long long stride, int c0, int c1, T& sum)
+{
+    bool ok = true, again = false;
+    for (int b = c0; b < c1;) {
+        unsigned long long pv[kBatchRecords];
+        bool empty = false;
+#pragma unroll
+        for (int u = 0; u < kBatchRecords; u++) {
+            pv[u] = (b + u < c1) ? ld_rec(base + (b + u) * stride) : 0ull;
+            empty |= pv[u] == kRecEmpty;
+        }
+        if (empty && !again) {   // rare: a store of this batch is still in flight; wait, then read it again
+            ok = poll_records(base, stride, b, min(b + kBatchRecords, c1)) && ok;
+            again = true;
+            continue;
+        }
+        again = false;
+        ok = ok && !empty;
+#pragma unroll
+        for (int u = 0; u < kBatchRecords; u++)
+            if (b + u < c1) rec_add(sum, pv[u] == kRecEmpty ? kRecNaN : pv[u]);
+        b += kBatchRecords;
+    }
+    for (int c = c0; c < c1; c++) st_rec(base + c * stride, kRecEmpty);   // empty again for the next launch
+    return ok;
+}
 
 // 8-byte asynchronous copy global -> shared (cp.async, no register held while
 // the copy is in flight), its commit and the wait for all of a thread's copies.
@@ -118,6 +203,7 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 // Waits until at most the most recent group of the thread's copies is in flight.
 __device__ __forceinline__ void cp_async_wait_prior() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
 // Release / acquire at GPU scope (the writes of the whole CTA are ordered
 // before it by the preceding barrier; fences are cumulative).
 __device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;\n" ::: "memory"); }
@@ -735,11 +821,17 @@ __global__ void __launch_bounds__(kTile, PK ? 6 : (VT >= 0 ? 7 : 6)) k_stage(con
     // ---- source chunks of one sink tile.  In a cluster launch (FP32 modes) the
     // tile's kClusterChunks chunks are the CTAs of one cluster: each leaves its
     // partial in its shared memory and chunk 0 sums them through distributed
-    // shared memory, in chunk order.  Otherwise the CTA that finishes last sums
+    // shared memory, in chunk order.  Otherwise the CTA that counts last sums
     // the partial records in global memory, every thread of it on a contiguous
     // range of chunks, in a fixed order; the chunk counter is advanced by the
-    // last thread, which holds no element (3 nsink <= 96 < kTile).  The element
-    // threads form the star term meanwhile ----
+    // last thread, which holds no element (3 nsink <= 96 < kTile).  The
+    // one-wave instance counts without fences and re-reads a record until it
+    // has landed: its launch is the critical chain of a try, and a release
+    // and an acquire fence cost ~1.2 us there.  The many-wave instances keep
+    // the fences, whose latency other CTAs hide, so that their reducing CTA
+    // never waits on a store in flight.  The element threads form the star
+    // term meanwhile ----
+    constexpr bool kFencedRecords = VT >= 0;
     float2 g_ds = make_float2(0.f, 0.f);   // gravity of the element, FP32 modes
     double a = 0.0;                         // gravity of the element, FP64 modes
     float2* acc2 = reinterpret_cast<float2*>(sm.acc);
@@ -750,15 +842,19 @@ __global__ void __launch_bounds__(kTile, PK ? 6 : (VT >= 0 ? 7 : 6)) k_stage(con
     } else if (it.nchunk > 1) {
         if (mine_ok) {
             const long long rec = 3 * ((long long)it.part_off + (long long)it.chunk * it.nsink) + 3 * mine_k + mine_c;
-            if (kF32) reinterpret_cast<float2*>(P.partial)[rec] = mine_ds;
-            else P.partial[rec] = mine;
+            if constexpr (!kFencedRecords) {
+                st_rec(reinterpret_cast<unsigned long long*>(P.partial) + rec, kF32 ? rec_bits(mine_ds) : rec_bits(mine));
+            } else {
+                if (kF32) reinterpret_cast<float2*>(P.partial)[rec] = mine_ds;
+                else P.partial[rec] = mine;
+            }
         }
         __syncthreads();
         if (t == kTile - 1) {
-            fence_acq_rel_gpu();   // release the CTA's partial record
+            if (kFencedRecords) fence_acq_rel_gpu();   // release the CTA's partial records
             const unsigned prev = atomicAdd(&P.tile_cnt[it.tile], 1u);
             const bool last = prev == (unsigned)(it.nchunk - 1);
-            if (last) fence_acq_rel_gpu();   // acquire the other chunks' records
+            if (kFencedRecords && last) fence_acq_rel_gpu();   // acquire the other chunks' records
             sm.flag = last;
         }
     }
@@ -816,11 +912,23 @@ __global__ void __launch_bounds__(kTile, PK ? 6 : (VT >= 0 ? 7 : 6)) k_stage(con
         const int e = t - sp_i * nel;
         const int c0 = sp_i < nsplit ? sp_i * it.nchunk / nsplit : 0;
         const int c1 = sp_i < nsplit ? (sp_i + 1) * it.nchunk / nsplit : 0;
-        const long long base = 3 * (long long)it.part_off + e;
-        if (kF32) {
-            acc2[t] = sum_records_ds(reinterpret_cast<const float2*>(P.partial) + base, 3LL * it.nsink, c0, c1);
+        if constexpr (kFencedRecords) {
+            const long long base = 3 * (long long)it.part_off + e;
+            if (kF32) acc2[t] = sum_records_ds(reinterpret_cast<const float2*>(P.partial) + base, 3LL * it.nsink, c0, c1);
+            else sm.acc[t] = sum_records(P.partial + base, 3LL * it.nsink, c0, c1);
         } else {
-            sm.acc[t] = sum_records(P.partial + base, 3LL * it.nsink, c0, c1);
+            unsigned long long* recs = reinterpret_cast<unsigned long long*>(P.partial) + 3 * (long long)it.part_off + e;
+            bool landed;
+            if (kF32) {
+                float2 sum = make_float2(0.f, 0.f);
+                landed = sum_polled_records(recs, 3LL * it.nsink, c0, c1, sum);
+                acc2[t] = sum;
+            } else {
+                double sum = 0.0;
+                landed = sum_polled_records(recs, 3LL * it.nsink, c0, c1, sum);
+                sm.acc[t] = sum;
+            }
+            if (!landed) S->status = 4;   // RED_ERR_TIMEOUT
         }
         __syncthreads();
         if (elem) {
@@ -844,51 +952,90 @@ __global__ void __launch_bounds__(kTile, PK ? 6 : (VT >= 0 ? 7 : 6)) k_stage(con
     if (kF32) a = dsn_to_double(dsn_add(g_ds, star_ds));
 
     cp_async_wait_all();
-    if (!elem) return;
 
     // ---- element-wise FP64 epilogue ----
-    const double vs = need_vs ? ops[kOpVS][t] : 0.0;   // stage velocity of the element
-    if (!(idi > 0)) a = 0.0;   // calc_grav_accel_naive zeroes inactive sinks (pp_disk.cu:386-388)
-    if (drag_act) {
-        const double g = ce == 0 ? sm.sc[ke][1] : (ce == 1 ? sm.sc[ke][2] : 0.0);
-        a = add<EXACT>(a, mul<EXACT>(sm.sc[ke][0], sub<EXACT>(g, vs)));   // a[i] += f u (pp_disk.cu:516-518)
-    }
-    P.Kv[s][x] = a;
-
-    if (V >= 1 && V <= 14) {
-        const double yr = ops[kOpYR][t], yv = ops[kOpYV][t];
-        double orr, ovv;
+    // The combinations of variants 1 .. 14 for element e: the positions
+    // y_r + dt sum_q a_q K_r,q from the stage velocity vse, and the velocities
+    // y_v + dt sum_q a_q K_v,q from the element's acceleration ae.
+    auto comb_r = [&](int e, double vse) -> double {
+        const double yr = ops[kOpYR][e];
         if (kRkf) {
             // ytemp of stage V: y + dt * sum_q a_{V,q} K_q, terms in red's order
             // (rk8_kernel::calc_ytemp_for_f1..f12, int_rungekutta8.cu:80-246)
             const int off = 1 + V * (V - 1) / 2;
-            const int s0 = op_src<VT>(V, 0);
-            const double kv0 = (s0 == V - 1) ? a : ops[kOpKV][t];
-            double ar = mul<EXACT>(c_tb.a[off + s0], ops[kOpKR][t]);
-            double av = mul<EXACT>(c_tb.a[off + s0], kv0);
+            double ar = mul<EXACT>(c_tb.a[off + op_src<VT>(V, 0)], ops[kOpKR][e]);
 #pragma unroll kUnroll
-            for (int q = 1; q < nk; q++) {
-                const int sq = op_src<VT>(V, q);
-                const double aq = c_tb.a[off + sq];
-                const double kvq = (sq == V - 1) ? a : ops[kOpKV + q][t];
-                ar = madd<EXACT>(ar, aq, ops[kOpKR + q][t]);
-                av = madd<EXACT>(av, aq, kvq);
-            }
-            orr = madd<EXACT>(yr, dt, ar);
-            ovv = madd<EXACT>(yv, dt, av);
+            for (int q = 1; q < nk; q++) ar = madd<EXACT>(ar, c_tb.a[off + op_src<VT>(V, q)], ops[kOpKR + q][e]);
+            return madd<EXACT>(yr, dt, ar);
         } else if (V == 13) {
             // rk4_kernel::sum_vector, int_rungekutta4.cu:36-47: y + (a dt) K_s
             const double bf = mul<EXACT>(P.scheme == SCHEME_RK2 ? c_tb.a2[s + 1] : c_tb.a4[s + 1], dt);
-            orr = madd<EXACT>(yr, bf, vs);
-            ovv = madd<EXACT>(yv, bf, a);
+            return madd<EXACT>(yr, bf, vse);
         } else {
             // RK4 y_{n+1} as the positions of the adaptive stage 4
             const double b0 = mul<EXACT>(c_tb.b4[0], dt), b1 = mul<EXACT>(c_tb.b4[1], dt);
-            orr = rk4_ynp1<EXACT>(yr, b0, b1, ops[kOpKR][t], ops[kOpKR + 1][t], ops[kOpKR + 2][t], vs);
-            ovv = rk4_ynp1<EXACT>(yv, b0, b1, ops[kOpKV][t], ops[kOpKV + 1][t], ops[kOpKV + 2][t], a);
+            return rk4_ynp1<EXACT>(yr, b0, b1, ops[kOpKR][e], ops[kOpKR + 1][e], ops[kOpKR + 2][e], vse);
         }
+    };
+    auto comb_v = [&](int e, double ae) -> double {
+        const double yv = ops[kOpYV][e];
+        if (kRkf) {
+            const int off = 1 + V * (V - 1) / 2;
+            const int s0 = op_src<VT>(V, 0);
+            double av = mul<EXACT>(c_tb.a[off + s0], (s0 == V - 1) ? ae : ops[kOpKV][e]);
+#pragma unroll kUnroll
+            for (int q = 1; q < nk; q++) {
+                const int sq = op_src<VT>(V, q);
+                av = madd<EXACT>(av, c_tb.a[off + sq], (sq == V - 1) ? ae : ops[kOpKV + q][e]);
+            }
+            return madd<EXACT>(yv, dt, av);
+        } else if (V == 13) {
+            const double bf = mul<EXACT>(P.scheme == SCHEME_RK2 ? c_tb.a2[s + 1] : c_tb.a4[s + 1], dt);
+            return madd<EXACT>(yv, bf, ae);
+        } else {
+            const double b0 = mul<EXACT>(c_tb.b4[0], dt), b1 = mul<EXACT>(c_tb.b4[1], dt);
+            return rk4_ynp1<EXACT>(yv, b0, b1, ops[kOpKV][e], ops[kOpKV + 1][e], ops[kOpKV + 2][e], ae);
+        }
+    };
+    // The one-wave instance with at most kTile / 2 elements (the large-body
+    // tiles, whose epilogue ends the launch) forms the position and velocity
+    // combinations of an element on two threads, t and t + kTile / 2, in
+    // different warps: each warp issues half the FP64 instructions.  The
+    // acceleration passes through sm.acc, whose slot t only thread t has read.
+    if constexpr (VT >= 0) {
+        if (!elem) return;
+    }
+    const double vs = (elem && need_vs) ? ops[kOpVS][t] : 0.0;   // stage velocity of the element
+    if (elem) {
+        if (!(idi > 0)) a = 0.0;   // calc_grav_accel_naive zeroes inactive sinks (pp_disk.cu:386-388)
+        if (drag_act) {
+            const double g = ce == 0 ? sm.sc[ke][1] : (ce == 1 ? sm.sc[ke][2] : 0.0);
+            a = add<EXACT>(a, mul<EXACT>(sm.sc[ke][0], sub<EXACT>(g, vs)));   // a[i] += f u (pp_disk.cu:516-518)
+        }
+        P.Kv[s][x] = a;
+    }
+    if (VT < 0 && V >= 1 && V <= 14 && 2 * nel <= kTile) {   // uniform over the CTA
+        if (elem) sm.acc[t] = a;
+        __syncthreads();   // the accelerations and every element's cp.async operands
+        const bool vside = t >= kTile / 2;
+        const int e = vside ? t - kTile / 2 : t;
+        if (e >= nel) return;
+        const int xe = 3 * it.sink0 + e;
+        if (vside) {
+            P.Kr[P.next][xe] = comb_v(e, sm.acc[e]);
+        } else {
+            const double orr = comb_r(e, need_vs ? ops[kOpVS][e] : 0.0);
+            P.r_out[xe] = orr;
+            write_pos_c(P.pos_hi_out, P.pos_lo_out, it.sink0 + e / 3, e % 3, orr);   // k_prep holds the .w words
+        }
+        return;
+    }
+    if (!elem) return;
+
+    if (V >= 1 && V <= 14) {
+        const double orr = comb_r(t, vs);
         P.r_out[x] = orr;
-        P.Kr[P.next][x] = ovv;
+        P.Kr[P.next][x] = comb_v(t, a);
         write_pos_c(P.pos_hi_out, P.pos_lo_out, ie, ce, orr);   // x, y, z; k_prep holds the .w words
     } else if (V == 15 || V == 16) {
         double e = 0.0;
