@@ -2153,7 +2153,7 @@ int red_autotune(red_sim* sim)
     struct Cand { int chunk, lanes; bool cluster, packed; };
     std::vector<Cand> cands;
     for (int lanes : {32, 16, 8}) {
-        cands.push_back({0, lanes, true, true});
+        cands.push_back({0, lanes, true, false});   // a cluster plan never takes the packed instance
         for (bool pk : {true, false}) {
             cands.push_back({0, lanes, false, pk});
             for (int c : {256, 512, 1024, 2048, 4096}) cands.push_back({c, lanes, false, pk});

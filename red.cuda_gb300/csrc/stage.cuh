@@ -111,11 +111,12 @@ __device__ __forceinline__ double sum_records(const double* base, long long stri
 // slot it read to kRecEmpty for the next launch.  Every store it waits for has
 // been issued (the chunk's CTA passed a barrier after its stores, then
 // counted), so the wait ends within the memory system's latency; it is bounded
-// all the same: after kRecPollLimit reads a record counts as NaN and the
-// system's status is set to RED_ERR_TIMEOUT.  (The many-wave instances keep a
-// release fence before the count and an acquire fence after the last one, and
-// plain records: the fences' latency hides behind other CTAs there, and their
-// reducing CTAs would otherwise meet stores in flight.)
+// all the same: after kRecPollLimit reads a record counts as NaN, the
+// system's status is set to RED_ERR_TIMEOUT and the system is halted.  (The
+// many-wave instances keep a release fence before the count and an acquire
+// fence after the last one, and plain records: the fences' latency hides
+// behind other CTAs there, and their reducing CTAs would otherwise meet
+// stores in flight.)
 constexpr unsigned long long kRecNaN = 0x7ff800007fc00000ull;   // NaN as a double and in both float halves
 constexpr int kRecPollLimit = 1 << 20;
 
@@ -928,7 +929,10 @@ __global__ void __launch_bounds__(kTile, PK ? 6 : (VT >= 0 ? 7 : 6)) k_stage(con
                 landed = sum_polled_records(recs, 3LL * it.nsink, c0, c1, sum);
                 sm.acc[t] = sum;
             }
-            if (!landed) S->status = 4;   // RED_ERR_TIMEOUT
+            if (!landed) {   // RED_ERR_TIMEOUT; the system stops (k_control then leaves it alone)
+                S->status = 4;
+                S->halted = 1;
+            }
         }
         __syncthreads();
         if (elem) {
