@@ -13,7 +13,7 @@ count per workload makes a step last ~50 ms, so that the timed region spans
 about a second and the clock record covers it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--config c2|c1|c3|c4|c5|dense|cube] [--precision mixed|fp64|fp32|fp64_exact]
+                  [--config c2|c1|c3|c4|c5|dense|cube|cube65536] [--precision mixed|fp64|fp32|fp64_exact]
                   [--accuracy-years T] [--plan-only]
 
 Timing: CUDA events on the integration stream around each step, L2 flushed
@@ -52,10 +52,10 @@ METRIC = "interactions/s and sim-years/s vs plain FP64 on same GPU at |ΔE/E|≤
 
 # tries per timed step (~50 ms of GPU time each) and untimed tries before the
 # timed region that take the step size past its start-up adaptation
-TRIES_PER_STEP = {"c1": 1000, "c2": 400, "c3": 120, "c4": 20, "c5": 20, "dense": 20, "cube": 60}
-SETTLE_TRIES = {"c1": 0, "c2": 600, "c3": 200, "c4": 200, "c5": 400, "dense": 100, "cube": 0}
+TRIES_PER_STEP = {"c1": 1000, "c2": 400, "c3": 120, "c4": 20, "c5": 20, "dense": 20, "cube": 60, "cube65536": 6}
+SETTLE_TRIES = {"c1": 0, "c2": 600, "c3": 200, "c4": 200, "c5": 400, "dense": 100, "cube": 0, "cube65536": 0}
 # steps of red's own GPU path per system (it is slower), and the ensemble's sample
-RED_GPU_STEPS = {"c1": 200, "c2": 20, "c3": 4, "c4": 6, "c5": 6, "dense": 4, "cube": 10}
+RED_GPU_STEPS = {"c1": 200, "c2": 20, "c3": 4, "c4": 6, "c5": 6, "dense": 4, "cube": 10, "cube65536": 1}
 RED_GPU_ENSEMBLE_SAMPLE = 16
 
 
@@ -93,10 +93,11 @@ def workload(rg, name, rank=0, world=1):
         return [s], dict(integrator="rkf78", adaptive=True, tolerance=1e-10, dt=1.0 * K_GAUSS,
                          collision_factor=0.0), \
             "config2 relabelled all-SI (every pair interacts, N = 16384), RKF7(8) tol 1e-10"
-    if name == "cube":
-        s = ic.benchmark_cube(16384)
+    if name in ("cube", "cube65536"):
+        n = 65536 if name == "cube65536" else 16384
+        s = ic.benchmark_cube(n)
         return [s], dict(integrator="rk4", adaptive=False, dt=1e-3, collision_factor=0.0), \
-            "red's benchmark cube: 16384 unit masses in [-50, 50]^3, all pairs, RK4 fixed step"
+            "red's benchmark cube: %d unit masses in [-50, 50]^3, all pairs, RK4 fixed step" % n
     s = ic.config2()
     return [s], dict(integrator="rkf78", adaptive=True, tolerance=1e-10, dt=1.0 * K_GAUSS,
                      collision_factor=1.0), \
@@ -803,7 +804,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "dense", "cube"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "dense", "cube", "cube65536"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp32", "fp64_exact"])
     ap.add_argument("--tries-per-step", type=int, default=0)
     ap.add_argument("--accuracy-years", type=float, default=0.0)

@@ -380,10 +380,13 @@ __device__ __forceinline__ void gravity_f32(SmemStage& sm, const StageParams& P,
 
 // The same gravity for tiles of 2 sinks per thread on 8 lanes, with packed
 // FP32 pairs (add / mul / fma .f32x2: one instruction for two interactions).
-// The lanes step over pairs of sources.  Each tile, staged in shared memory
-// as one float4 per source, is first rewritten in place as pair records:
+// The lanes step over pairs of sources, held in shared memory as pair records:
 //   A[p] = (x_2p, x_2p+1, y_2p, y_2p+1), B[p] = (z_2p, z_2p+1, m_2p, m_2p+1)
 // and, for the double-single low parts, C[p] = (x, x', y, y') and D[p] = (z, z').
+// A chunk of up to two tiles, staged at once as one float4 per source, is
+// rewritten in place (pair_tiles); the tiles of a longer chunk go from the
+// registers that prefetch them straight into the records of two alternating
+// buffers (put_pair), one barrier per tile.
 // An odd source count pads the last pair with a copy of its first source of
 // mass 0 (its term is 0 * finite).  The sums are those of gravity_f32 in
 // another grouping: each lane's tile sum is the sum of its two pair halves.
@@ -423,6 +426,30 @@ __device__ __forceinline__ void pair_tiles(SmemStage& sm, int nsrc, int ntile)
     __syncthreads();
 }
 
+// Source t of a streamed tile, from registers straight into pair buffer buf
+// (sm.src.f.hi / .lo from buf * kTile): the records pair_tiles makes, with no
+// staging pass.  A source beyond the chunk comes as zeros (mass 0).
+template <int MODE>
+__device__ __forceinline__ void put_pair(SmemStage& sm, int buf, int t, float4 h, float4 l)
+{
+    constexpr int kHalf = kTile / 2;
+    float* A = reinterpret_cast<float*>(sm.src.f.hi + buf * kTile);
+    float* B = A + 4 * kHalf;
+    const int o = 4 * (t >> 1) + (t & 1);
+    A[o] = h.x;
+    A[o + 2] = h.y;
+    B[o] = h.z;
+    B[o + 2] = h.w;
+    if (MODE == MODE_MIXED) {
+        float* Cl = reinterpret_cast<float*>(sm.src.f.lo + buf * kTile);
+        float* Dl = Cl + 4 * kHalf;
+        Cl[o] = l.x;
+        Cl[o + 2] = l.y;
+        Dl[o] = l.z;
+        Dl[o + 2] = 0.f;
+    }
+}
+
 template <int MODE>
 __device__ __forceinline__ void gravity_f32_pair(SmemStage& sm, const StageParams& P, const GravItem& it,
                                                  bool staged, float4& th, float4& tl, float2& mine, int& mine_k,
@@ -451,15 +478,16 @@ __device__ __forceinline__ void gravity_f32_pair(SmemStage& sm, const StageParam
 #pragma unroll
         for (int c = 0; c < 6; c++) acc[q][c] = 0.f;
     if (staged) pair_tiles<MODE>(sm, it.src1 - it.src0, (it.src1 - it.src0 + kTile - 1) / kTile);
+    int buf = 0;   // streamed chunks: the pair buffer of the current tile (the prologue filled buffer 0)
     for (int j0 = it.src0; j0 < it.src1; j0 += kTile) {
         const int nj = min(kTile, it.src1 - j0);
         const bool more = !staged && j0 + kTile < it.src1;
-        const int base = staged ? j0 - it.src0 : 0;   // staged chunks hold all their tiles
-        if (more && t < min(kTile, it.src1 - j0 - kTile)) {
+        const int nnext = more ? min(kTile, it.src1 - j0 - kTile) : 0;
+        const int base = staged ? j0 - it.src0 : buf * kTile;   // staged chunks hold all their tiles
+        if (t < nnext) {
             th = P.pos_hi_in[j0 + kTile + t];
             if (MODE == MODE_MIXED) tl = P.pos_lo_in[j0 + kTile + t];
         }
-        if (!staged) pair_tiles<MODE>(sm, nj, 1);
         const float4* A = sm.src.f.hi + base;
         const float4* B = A + kHalf;
         const float4* Cl = sm.src.f.lo + base;
@@ -504,10 +532,12 @@ __device__ __forceinline__ void gravity_f32_pair(SmemStage& sm, const StageParam
             ds_add(acc[q][4], acc[q][5], tz[q].x + tz[q].y);
         }
         if (more) {
+            // the next tile goes into the other buffer, which every thread finished
+            // reading before the barrier that ended the previous tile
+            if (t >= nnext) th = tl = make_float4(0.f, 0.f, 0.f, 0.f);
+            put_pair<MODE>(sm, buf ^ 1, t, th, tl);
             __syncthreads();
-            sm.src.f.hi[t] = th;
-            if (MODE == MODE_MIXED) sm.src.f.lo[t] = tl;
-            __syncthreads();
+            buf ^= 1;
         }
     }
     for (int o = 1; o < L; o <<= 1) {
@@ -795,8 +825,12 @@ __global__ void __launch_bounds__(kTile, PK ? 6 : (VT >= 0 ? 7 : 6)) k_stage(con
     }
     if (kF32) {
         if (!staged) {
-            sm.src.f.hi[t] = th;
-            if (MODE == MODE_MIXED) sm.src.f.lo[t] = tl;
+            if (PK && it.spt == 2) {   // the packed-pair loop streams its tiles as pair records
+                put_pair<MODE>(sm, 0, t, th, tl);
+            } else {
+                sm.src.f.hi[t] = th;
+                if (MODE == MODE_MIXED) sm.src.f.lo[t] = tl;
+            }
         }
     } else {
         sm.src.d.d[t] = td;

@@ -166,10 +166,17 @@ def _p(a):
     return a.ctypes.data_as(C.c_void_p)
 
 
+def _addr(a):
+    """The address of a numpy array's data, for a c_void_p argument (cheaper
+    than a ctypes pointer object on the per-step state calls)."""
+    return a.ctypes.data
+
+
 def _check_out(a, dtype, n):
     """An array the library writes n records of `dtype` into: contiguous, of
     that exact layout (a packed copy of a padded record would be overrun)."""
-    if not a.flags["C_CONTIGUOUS"] or len(a) != n or a.dtype != dtype or a.dtype.itemsize != dtype.itemsize:
+    if not a.flags.c_contiguous or len(a) != n or not (a.dtype is dtype or (a.dtype == dtype and
+                                                                            a.dtype.itemsize == dtype.itemsize)):
         raise ValueError("out arrays must be contiguous with %d records of %s" % (n, dtype))
 
 
@@ -377,7 +384,10 @@ class Sim:
     def bodies(self, sys0=0, count=None):
         """Bodies of the systems [sys0, sys0 + count) (all from sys0 by default)."""
         count = self.n_systems - sys0 if count is None else count
-        return sum(int(load().red_n_bodies(self.h, k)) for k in range(sys0, sys0 + count))
+        L = load()
+        if count == 1:
+            return int(L.red_n_bodies(self.h, sys0))
+        return sum(int(L.red_n_bodies(self.h, k)) for k in range(sys0, sys0 + count))
 
     def get_states(self, out, sys0=0, count=None, parts="rvpm"):
         """The records of systems [sys0, sys0 + count), one system after the other,
@@ -385,11 +395,13 @@ class Sim:
         bodies(sys0, count) records) in one call; returns out."""
         count = self.n_systems - sys0 if count is None else count
         n = self.bodies(sys0, count)
-        arrs = [(out.r, "r"), (out.v, "v"), (out.p, "p"), (out.md, "m")]
-        for (a, k), t in zip(arrs, (VAR4, VAR4, PARAM, BMD)):
+        ptrs = [None, None, None, None]
+        for i, (a, t, k) in enumerate(((out.r, VAR4, "r"), (out.v, VAR4, "v"), (out.p, PARAM, "p"),
+                                       (out.md, BMD, "m"))):
             if k in parts:
                 _check_out(a, t, n)
-        _check(load().red_get_states(self.h, sys0, count, *[_p(a) if k in parts else None for a, k in arrs]))
+                ptrs[i] = _addr(a)
+        _check(load().red_get_states(self.h, sys0, count, *ptrs))
         return out
 
     def set_states(self, s, sys0=0, count=None, parts="rvpm"):
@@ -397,12 +409,16 @@ class Sim:
         [sys0, sys0 + count), one system after the other) in one call."""
         count = self.n_systems - sys0 if count is None else count
         n = self.bodies(sys0, count)
-        arrs = [(s.r, VAR4, "r"), (s.v, VAR4, "v"), (s.p, PARAM, "p"), (s.md, BMD, "m")]
-        keep = [np.ascontiguousarray(a, t) if k in parts else None for a, t, k in arrs]
-        for a in keep:
-            if a is not None and len(a) != n:
-                raise ValueError("arrays must hold %d records" % n)
-        _check(load().red_set_states(self.h, sys0, count, *[_p(a) if a is not None else None for a in keep]))
+        keep = [None, None, None, None]   # the (contiguous) arrays stay referenced during the call
+        ptrs = [None, None, None, None]
+        for i, (a, t, k) in enumerate(((s.r, VAR4, "r"), (s.v, VAR4, "v"), (s.p, PARAM, "p"), (s.md, BMD, "m"))):
+            if k in parts:
+                a = np.ascontiguousarray(a, t)
+                if len(a) != n:
+                    raise ValueError("arrays must hold %d records" % n)
+                keep[i] = a
+                ptrs[i] = _addr(a)
+        _check(load().red_set_states(self.h, sys0, count, *ptrs))
 
     def set_dt_next(self, sys, dt):
         _check(load().red_set_dt_next(self.h, sys, dt))
