@@ -111,11 +111,11 @@ __device__ __forceinline__ double sum_records(const double* base, long long stri
 // slot it read to kRecEmpty for the next launch.  Every store it waits for has
 // been issued (the chunk's CTA passed a barrier after its stores, then
 // counted), so the wait ends within the memory system's latency; it is bounded
-// all the same: after kRecPollLimit reads a record counts as NaN, the
-// system's status is set to RED_ERR_TIMEOUT and the system is halted.  (The
-// many-wave instances keep a release fence before the count and an acquire
-// fence after the last one, and plain records: the fences' latency hides
-// behind other CTAs there, and their reducing CTAs would otherwise meet
+// all the same: after kRecPollLimit reads of a batch its missing records count
+// as NaN, the system's status is set to RED_ERR_TIMEOUT and the system is
+// halted.  (The many-wave instances keep a release fence before the count and
+// an acquire fence after the last one, and plain records: the fences' latency
+// hides behind other CTAs there, and their reducing CTAs would otherwise meet
 // stores in flight.)
 constexpr unsigned long long kRecNaN = 0x7ff800007fc00000ull;   // NaN as a double and in both float halves
 constexpr int kRecPollLimit = 1 << 20;
@@ -141,17 +141,21 @@ __device__ __forceinline__ void rec_add(float2& a, unsigned long long b)
 }
 __device__ __forceinline__ void rec_add(double& a, unsigned long long b) { a += __longlong_as_double((long long)b); }
 
-// Re-reads the records [b, b1) until every chunk's store has landed (at most
-// kRecPollLimit reads each).  Returns false if one never does.
+// Re-reads the records [b, b1) until every chunk's store has landed, within
+// one budget of kRecPollLimit reads for the whole batch.  Returns false if
+// the budget runs out first.
 __device__ __forceinline__ bool poll_records(const unsigned long long* base, long long stride, int b, int b1)
 {
-    bool ok = true;
+    int budget = kRecPollLimit;
     for (int c = b; c < b1; c++) {
         unsigned long long v = kRecEmpty;
-        for (int n = 0; v == kRecEmpty && n < kRecPollLimit; n++) v = ld_rec(base + c * stride);
-        ok = ok && v != kRecEmpty;
+        while (v == kRecEmpty && budget > 0) {
+            v = ld_rec(base + c * stride);
+            budget--;
+        }
+        if (v == kRecEmpty) return false;
     }
-    return ok;
+    return true;
 }
 
 // Sum of the polled records [c0, c1) of one element (element t of the tile at
