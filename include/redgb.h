@@ -274,8 +274,7 @@ int red_populate_disks(const red_disk_spec_t* specs, uint32_t n_systems, int32_t
  * library, held by every GPU that loads it until exit; calls share it, so
  * calls that overlap on the GPU race and must be ordered by the caller.  The
  * first call on a device does a one-time set-up (it looks up the device
- * address of the array): make that first call before any stream capture.
- * The call writes no constant memory, so simulations created earlier keep
+ * address of the array).  The call writes no constant memory, so simulations created earlier keep
  * their integrator coefficients.  Every system of up to
  * RED_NOALLOC_MAX_BODIES bodies fits, whatever its body classes (a plan that
  * would need more partial-sum records than the array holds falls back to

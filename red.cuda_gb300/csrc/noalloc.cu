@@ -16,8 +16,8 @@
 // race on it -- callers must order them.
 //
 // The first call on a device looks up the device address of the array with
-// cudaGetSymbolAddress (with that device current); make that first call
-// before any stream capture.  The entry point writes no constant memory: a
+// cudaGetSymbolAddress (with that device current).  The entry point writes no
+// constant memory: a
 // standalone evaluation reads no integrator coefficients, and the tableau
 // that live simulations loaded stays as it is.
 //
