@@ -17,9 +17,8 @@
 //
 // The first call on a device looks up the device address of the array with
 // cudaGetSymbolAddress (with that device current).  The entry point writes no
-// constant memory: a
-// standalone evaluation reads no integrator coefficients, and the tableau
-// that live simulations loaded stays as it is.
+// constant memory: a standalone evaluation reads no integrator coefficients,
+// and the tableau that live simulations loaded stays as it is.
 //
 // Every system of at most RED_NOALLOC_MAX_BODIES bodies fits: when the
 // allocating path's launch plan (sources split into chunks whose partial sums
