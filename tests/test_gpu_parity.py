@@ -467,3 +467,31 @@ def test_gravity_packed_pairs(rg, orc, monkeypatch, precision, bound):
         assert err[0] < 2e-6 and err[1:].max() < bound, (packed, err[0], err[1:].max())
     d = np.linalg.norm(out["1"][0] - out["0"][0], axis=1) / np.linalg.norm(ref, axis=1)
     assert d[1:].max() < bound
+
+
+@pytest.mark.parametrize("precision,bound", [("mixed", 1e-8), ("fp32", 5e-7)])
+def test_gravity_packed_pairs_streamed(rg, orc, monkeypatch, precision, bound):
+    """The packed instance with chunks longer than the two-tile staging
+    buffer: each prefetched tile goes straight into the pair records of the
+    other of two buffers.  An all-SI disk of 16401 bodies, whose heuristic
+    plan cuts every tile's sources into ~14 chunks of nine tiles (the last
+    chunk 273 sources, so its last tile has an odd count and a padded pair),
+    against the FP64 oracle and the scalar instance as in
+    test_gravity_packed_pairs."""
+    s = rg.ic.config2(seed=45, n_pp=16, n_pl=16384).relabel_all_SI()
+    out = {}
+    for packed in ("1", "0"):
+        monkeypatch.setenv("REDGB_PACKED", packed)
+        with rg.Sim(s, dt=0.01, precision=precision) as sim:
+            out[packed] = (vec(sim.calc_dydx(0, 1, 0.0)), sim.plan_info())
+    info = out["1"][1]
+    tiles = (s.n + 31) // 32
+    assert info["packed"] and info["n_items"] <= 20 * tiles   # chunks of > 2 tiles of 128 sources
+    _, ref = orc.grav_accel(obody(orc, s), sem=orc.SEM_GPU, nthreads=16)
+    ref = vec(ref)
+    for packed in ("1", "0"):
+        a = out[packed][0]
+        err = np.linalg.norm(a - ref, axis=1) / np.linalg.norm(ref, axis=1)
+        assert err[0] < 2e-6 and err[1:].max() < bound, (packed, err[0], err[1:].max())
+    d = np.linalg.norm(out["1"][0] - out["0"][0], axis=1) / np.linalg.norm(ref, axis=1)
+    assert d[1:].max() < bound
