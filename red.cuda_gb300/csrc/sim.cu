@@ -408,6 +408,7 @@ struct red_sim {
     // host transfers: device records (k_pack_state layout) and a pinned host copy
     char* d_xfer = nullptr;
     char* h_xfer = nullptr;
+    DevSys* h_sys = nullptr;   // page-locked copy of the system records (read_sys)
     size_t xfer_cap = 0;
     void ensure_xfer(size_t bytes);
     void pack_range_to_host(size_t o, size_t n);   // bodies [o, o + n) into h_xfer
@@ -517,6 +518,7 @@ red_sim::~red_sim()
     cudaFree(d_grid); cudaFree(d_head); cudaFree(d_next); cudaFree(d_cell); cudaFree(d_fsegs);
     cudaFree(d_xfer);
     if (h_xfer) cudaFreeHost(h_xfer);
+    if (h_sys) cudaFreeHost(h_sys);
     cudaFree(d_mlp_w); cudaFree(d_fpart); cudaFree(d_seg0); cudaFree(d_nseg); cudaFree(d_feat_prev);
     cudaFree(d_has_prev); cudaFree(d_log); cudaFree(d_log_n);
     if (own_stream && stream) cudaStreamDestroy(stream);
@@ -1120,9 +1122,12 @@ bool red_sim::launch_sparse_try(const std::vector<DevSys>& ds)
 
 void red_sim::read_sys(std::vector<DevSys>& out)
 {
-    out.resize(n_sys);
-    CK(cudaMemcpyAsync(out.data(), d_sys, n_sys * sizeof(DevSys), cudaMemcpyDeviceToHost, stream));
+    // through page-locked memory: a DMA copy with no staging by the driver
+    // (red_step reads the records after every try)
+    if (!h_sys) CK(cudaMallocHost(&h_sys, n_sys * sizeof(DevSys)));
+    CK(cudaMemcpyAsync(h_sys, d_sys, n_sys * sizeof(DevSys), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
+    out.assign(h_sys, h_sys + n_sys);
 }
 
 void red_sim::write_sys(const std::vector<DevSys>& in)
